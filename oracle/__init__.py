@@ -1,0 +1,347 @@
+"""ORACLE — test infrastructure only.
+
+ctypes bindings over the CPU restatement (``oracle/_build/liboracle.so``, built by
+``oracle/Makefile``) and, where it was built, over the reference's own compiled CPU solver
+(``oracle/_ref/libwsref.so``, built by ``oracle/build_ref.sh`` from the reference's sources).
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this
+package, always as the checker or the CPU baseline, never as the thing measured or shipped.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libwsref.so")
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_lib = None
+_ref = None
+
+
+def build(quiet: bool = True) -> None:
+    """Compiles the restatement (make -C oracle)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+
+
+def build_ref(reference_root: str = "/root/reference") -> bool:
+    """Compiles the reference's own solver when its sources are present; True if built."""
+    subprocess.run([os.path.join(HERE, "build_ref.sh"), reference_root], check=True,
+                   stdout=subprocess.DEVNULL)
+    return os.path.exists(REF_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.oracle_hash_floats.restype = C.c_uint64
+        L.oracle_hash_floats.argtypes = [_fp, C.c_size_t]
+        L.oracle_step_create.restype = C.c_void_p
+        L.oracle_step_create.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.c_uint32, C.c_int, C.c_int]
+        for name, args in [
+            ("oracle_step_destroy", [C.c_void_p]),
+            ("oracle_step_write_state", [C.c_void_p, _dp, _dp, _dp]),
+            ("oracle_step_set_bed", [C.c_void_p, _dp, C.c_double]),
+            ("oracle_step_set_manning", [C.c_void_p, _dp]),
+            ("oracle_step_set_source", [C.c_void_p, _dp, C.c_uint32, C.c_int]),
+            ("oracle_step_run_steps", [C.c_void_p, C.c_uint32, C.c_double]),
+            ("oracle_step_run_length_pass", [C.c_void_p, C.c_double]),
+            ("oracle_step_read_ledger", [C.c_void_p, _dp]),
+            ("oracle_step_read_state_f32", [C.c_void_p, _fp]),
+            ("oracle_step_read_state_f64", [C.c_void_p, _dp]),
+            ("oracle_step_write_planes_f32", [C.c_void_p, _fp]),
+            ("oracle_step_read_partials", [C.c_void_p, _fp]),
+            ("oracle_step_read_ledger_bits", [C.c_void_p, C.c_void_p]),
+        ]:
+            f = getattr(L, name)
+            f.restype = None
+            f.argtypes = args
+        L.oracle_step_advance.restype = C.c_uint64
+        L.oracle_step_advance.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_int)]
+        L.oracle_step_state_hash.restype = C.c_uint64
+        L.oracle_step_state_hash.argtypes = [C.c_void_p]
+        L.oracle_step_group_count.restype = C.c_uint32
+        L.oracle_step_group_count.argtypes = [C.c_void_p]
+        L.oracle_solver_create.restype = C.c_void_p
+        L.oracle_solver_create.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double,
+                                           C.c_double, C.c_double, C.c_uint32, C.c_uint32]
+        for name, args in [
+            ("oracle_solver_destroy", [C.c_void_p]),
+            ("oracle_solver_set_state", [C.c_void_p, _dp, _dp, _dp]),
+            ("oracle_solver_set_inputs", [C.c_void_p, _dp, _dp, _dp]),
+            ("oracle_solver_get_state", [C.c_void_p, _dp, _dp, _dp]),
+            ("oracle_solver_ledger", [C.c_void_p, _dp]),
+        ]:
+            f = getattr(L, name)
+            f.restype = None
+            f.argtypes = args
+        L.oracle_solver_step.restype = C.c_double
+        L.oracle_solver_step.argtypes = [C.c_void_p, C.c_double]
+        L.oracle_solver_advance.restype = C.c_uint64
+        L.oracle_solver_advance.argtypes = [C.c_void_p, C.c_double]
+        L.oracle_solver_state_hash.restype = C.c_uint64
+        L.oracle_solver_state_hash.argtypes = [C.c_void_p]
+        L.oracle_solver_volume.restype = C.c_double
+        L.oracle_solver_volume.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        R = C.CDLL(REF_PATH)
+        R.wsref_create.restype = C.c_void_p
+        R.wsref_create.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_uint32, C.c_uint32]
+        for name, args in [
+            ("wsref_destroy", [C.c_void_p]),
+            ("wsref_set_state", [C.c_void_p, _dp, _dp, _dp]),
+            ("wsref_set_inputs", [C.c_void_p, _dp, _dp, _dp]),
+            ("wsref_get_state", [C.c_void_p, _dp, _dp, _dp]),
+            ("wsref_ledger", [C.c_void_p, _dp]),
+        ]:
+            f = getattr(R, name)
+            f.restype = None
+            f.argtypes = args
+        R.wsref_step.restype = C.c_double
+        R.wsref_step.argtypes = [C.c_void_p, C.c_double]
+        R.wsref_advance.restype = C.c_uint64
+        R.wsref_advance.argtypes = [C.c_void_p, C.c_double]
+        R.wsref_state_hash.restype = C.c_uint64
+        R.wsref_state_hash.argtypes = [C.c_void_p]
+        R.wsref_volume.restype = C.c_double
+        R.wsref_volume.argtypes = [C.c_void_p]
+        _ref = R
+    return _ref
+
+
+def _d(a):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.ctypes.data_as(_dp)
+
+
+def _keep(*arrays):
+    return [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in arrays]
+
+
+@dataclass
+class Grid:
+    """The fields of water_state::Config the step reads (water_state.h:83-99)."""
+    nx: int
+    ny: int
+    cell_m: float = 1.0
+    gravity: float = 9.81
+    cfl: float = 0.45
+    dry_depth_m: float = 1e-9
+    open_edges: int = 0  # bits: 1 west, 2 east, 4 south, 8 north
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny
+
+
+class RefStep:
+    """The card's step on the CPU (water_step.slang + water_live.cpp's host half)."""
+
+    def __init__(self, grid: Grid, fixed_ops: bool = False, precision64: bool = False):
+        L = lib()
+        self.grid = grid
+        self.is64 = precision64
+        self.h = L.oracle_step_create(grid.nx, grid.ny, grid.cell_m, grid.gravity, grid.cfl,
+                                      grid.dry_depth_m, grid.open_edges, int(fixed_ops),
+                                      int(precision64))
+        if not self.h:
+            raise ValueError("oracle: an empty grid")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_step_destroy(self.h)
+            self.h = None
+
+    def write_state(self, h, hu, hv):
+        h, hu, hv = _keep(h, hu, hv)
+        lib().oracle_step_write_state(self.h, _d(h), _d(hu), _d(hv))
+
+    def set_bed(self, bed, datum=0.0):
+        (bed,) = _keep(bed)
+        lib().oracle_step_set_bed(self.h, _d(bed), float(datum))
+
+    def set_manning(self, m):
+        (m,) = _keep(m)
+        lib().oracle_step_set_manning(self.h, _d(m))
+
+    def set_source(self, s, every=1, compensate=False):
+        (s,) = _keep(s)
+        lib().oracle_step_set_source(self.h, _d(s), int(every), int(compensate))
+
+    def run_steps(self, count, max_dt):
+        lib().oracle_step_run_steps(self.h, int(count), float(max_dt))
+
+    def run_length_pass(self, max_dt):
+        lib().oracle_step_run_length_pass(self.h, float(max_dt))
+
+    def read_ledger(self):
+        out = np.zeros(6)
+        lib().oracle_step_read_ledger(self.h, out.ctypes.data_as(_dp))
+        return dict(source_m3=out[0], open_edge_out_m3=out[1], roundoff_m3=out[2],
+                    time_s=out[3], remaining_s=out[4], steps=int(out[5]))
+
+    def advance(self, duration):
+        refused = C.c_int(0)
+        steps = lib().oracle_step_advance(self.h, float(duration), C.byref(refused))
+        return steps, bool(refused.value)
+
+    def read_state_bits(self):
+        n = self.grid.cells
+        if self.is64:
+            out = np.zeros(4 * n, dtype=np.float64)
+            lib().oracle_step_read_state_f64(self.h, out.ctypes.data_as(_dp))
+        else:
+            out = np.zeros(4 * n, dtype=np.float32)
+            lib().oracle_step_read_state_f32(self.h, out.ctypes.data_as(_fp))
+        return out
+
+    def write_planes(self, planes):
+        p = np.ascontiguousarray(planes, dtype=np.float32)
+        lib().oracle_step_write_planes_f32(self.h, p.ctypes.data_as(_fp))
+
+    def state_hash(self):
+        return int(lib().oracle_step_state_hash(self.h))
+
+    def group_count(self):
+        return int(lib().oracle_step_group_count(self.h))
+
+    def read_partials_bits(self):
+        out = np.zeros(8 * self.group_count(), dtype=np.float32)
+        lib().oracle_step_read_partials(self.h, out.ctypes.data_as(_fp))
+        return out.reshape(-1, 8)
+
+    def read_ledger_bits(self):
+        out = np.zeros(12, dtype=np.uint32)
+        lib().oracle_step_read_ledger_bits(self.h, out.ctypes.data_as(C.c_void_p))
+        return out
+
+
+class Solver64:
+    """The reference CPU tick restated (water_state.cpp): depth and momenta, FP64."""
+
+    def __init__(self, grid: Grid, threads: int = 1):
+        self.grid = grid
+        self.h = lib().oracle_solver_create(grid.nx, grid.ny, grid.cell_m, grid.gravity,
+                                            grid.cfl, grid.dry_depth_m, grid.open_edges,
+                                            int(threads))
+        self._inputs = None
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_solver_destroy(self.h)
+            self.h = None
+
+    def set_state(self, h, hu=None, hv=None):
+        n = self.grid.cells
+        hu = np.zeros(n) if hu is None else hu
+        hv = np.zeros(n) if hv is None else hv
+        h, hu, hv = _keep(h, hu, hv)
+        lib().oracle_solver_set_state(self.h, _d(h), _d(hu), _d(hv))
+
+    def set_inputs(self, bed, manning=None, source=None):
+        bed, manning, source = _keep(bed, manning, source)
+        lib().oracle_solver_set_inputs(self.h, _d(bed), _d(manning), _d(source))
+
+    def step(self, max_dt):
+        return lib().oracle_solver_step(self.h, float(max_dt))
+
+    def advance(self, duration):
+        return int(lib().oracle_solver_advance(self.h, float(duration)))
+
+    def state(self):
+        n = self.grid.cells
+        h, hu, hv = np.zeros(n), np.zeros(n), np.zeros(n)
+        lib().oracle_solver_get_state(self.h, _d(h), _d(hu), _d(hv))
+        return h, hu, hv
+
+    def state_hash(self):
+        return int(lib().oracle_solver_state_hash(self.h))
+
+    def ledger(self):
+        out = np.zeros(5)
+        lib().oracle_solver_ledger(self.h, out.ctypes.data_as(_dp))
+        return dict(source_m3=out[0], open_edge_out_m3=out[1], roundoff_m3=out[2],
+                    time_s=out[3], steps=int(out[4]))
+
+    def volume(self):
+        return lib().oracle_solver_volume(self.h)
+
+
+class RefSolver:
+    """The reference's own compiled water_state::Solver (oracle/_ref), where it was built."""
+
+    def __init__(self, grid: Grid, workers: int = 0):
+        R = ref()
+        self.grid = grid
+        self.h = R.wsref_create(grid.nx, grid.ny, grid.cell_m, grid.gravity, grid.cfl,
+                                grid.dry_depth_m, grid.open_edges, int(workers))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref().wsref_destroy(self.h)
+            self.h = None
+
+    def set_state(self, h, hu=None, hv=None):
+        n = self.grid.cells
+        hu = np.zeros(n) if hu is None else hu
+        hv = np.zeros(n) if hv is None else hv
+        h, hu, hv = _keep(h, hu, hv)
+        ref().wsref_set_state(self.h, _d(h), _d(hu), _d(hv))
+
+    def set_inputs(self, bed, manning=None, source=None):
+        bed, manning, source = _keep(bed, manning, source)
+        self._inputs = (bed, manning, source)
+        ref().wsref_set_inputs(self.h, _d(bed), _d(manning), _d(source))
+
+    def step(self, max_dt):
+        return ref().wsref_step(self.h, float(max_dt))
+
+    def advance(self, duration):
+        return int(ref().wsref_advance(self.h, float(duration)))
+
+    def state(self):
+        n = self.grid.cells
+        h, hu, hv = np.zeros(n), np.zeros(n), np.zeros(n)
+        ref().wsref_get_state(self.h, _d(h), _d(hu), _d(hv))
+        return h, hu, hv
+
+    def state_hash(self):
+        return int(ref().wsref_state_hash(self.h))
+
+    def ledger(self):
+        out = np.zeros(5)
+        ref().wsref_ledger(self.h, out.ctypes.data_as(_dp))
+        return dict(source_m3=out[0], open_edge_out_m3=out[1], roundoff_m3=out[2],
+                    time_s=out[3], steps=int(out[4]))
+
+    def volume(self):
+        return ref().wsref_volume(self.h)
+
+
+def hash_floats(values) -> int:
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    return int(lib().oracle_hash_floats(v.ctypes.data_as(_fp), v.size))
