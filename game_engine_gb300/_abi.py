@@ -1,0 +1,92 @@
+"""ctypes declarations of include/wlcuda.h (the C ABI), kept beside the header's order."""
+from __future__ import annotations
+
+import ctypes as C
+
+wl_stream = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_err = [C.c_char_p, C.c_size_t]
+
+
+class Config(C.Structure):
+    """wl_config: water_state::Config's fields the step reads (water_state.h:83-99)."""
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("cell_m", C.c_double),
+                ("gravity", C.c_double), ("cfl", C.c_double), ("dry_depth_m", C.c_double),
+                ("west_open", C.c_uint8), ("east_open", C.c_uint8), ("south_open", C.c_uint8),
+                ("north_open", C.c_uint8), ("device", C.c_int32)]
+
+
+class Options(C.Structure):
+    """wl_options: StepOptions (water_live.h:105-110)."""
+    _fields_ = [("ops", C.c_uint8), ("stored_faces", C.c_uint8)]
+
+
+class StepParams(C.Structure):
+    """wl_step_params: StepParams (water_live.h:66-88), 120 bytes."""
+    _fields_ = [("state_in", C.c_uint64), ("state_out", C.c_uint64), ("bed", C.c_uint64),
+                ("manning", C.c_uint64), ("source", C.c_uint64), ("partials", C.c_uint64),
+                ("ledger", C.c_uint64), ("nx", C.c_uint32), ("ny", C.c_uint32),
+                ("groups_x", C.c_uint32), ("group_count", C.c_uint32), ("flags", C.c_uint32),
+                ("cell_m", C.c_float), ("gravity", C.c_float), ("cfl", C.c_float),
+                ("dry_depth_m", C.c_float), ("max_dt", C.c_float), ("source_scale", C.c_float),
+                ("pad", C.c_uint32), ("faces_x", C.c_uint64), ("faces_y", C.c_uint64)]
+
+
+class Partial(C.Structure):
+    """wl_partial: WaterPartial (water_live.h:114-121), 32 bytes."""
+    _fields_ = [("speed_x", C.c_float), ("speed_y", C.c_float), ("source_m3", C.c_float),
+                ("open_m3", C.c_float), ("roundoff_m3", C.c_float), ("pad", C.c_float * 3)]
+
+
+class LedgerBits(C.Structure):
+    """wl_ledger_bits: WaterLedger (water_live.h:124-137), 48 bytes."""
+    _fields_ = [("time_hi", C.c_float), ("time_lo", C.c_float), ("source_hi", C.c_float),
+                ("source_lo", C.c_float), ("open_hi", C.c_float), ("open_lo", C.c_float),
+                ("roundoff_hi", C.c_float), ("roundoff_lo", C.c_float),
+                ("remaining_s", C.c_float), ("dt", C.c_float), ("steps", C.c_uint32),
+                ("pad", C.c_uint32)]
+
+
+class Ledger(C.Structure):
+    """wl_ledger: water_live::Ledger (water_live.h:143-150)."""
+    _fields_ = [("source_m3", C.c_double), ("open_edge_out_m3", C.c_double),
+                ("roundoff_m3", C.c_double), ("time_s", C.c_double),
+                ("remaining_s", C.c_double), ("steps", C.c_uint64)]
+
+
+# name -> (restype, argtypes); every symbol include/wlcuda.h declares.
+SIGNATURES = {
+    "wl_create": (C.c_int, [C.POINTER(Config), C.POINTER(Options), C.POINTER(C.c_void_p), *_err]),
+    "wl_destroy": (None, [C.c_void_p]),
+    "wl_valid": (C.c_int, [C.c_void_p]),
+    "wl_cell_count": (C.c_uint32, [C.c_void_p]),
+    "wl_group_count": (C.c_uint32, [C.c_void_p]),
+    "wl_write_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
+    "wl_read_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
+    "wl_read_state_bits": (C.c_int, [C.c_void_p, _fp, C.c_size_t, *_err]),
+    "wl_read_ledger": (C.c_int, [C.c_void_p, C.POINTER(Ledger), *_err]),
+    "wl_set_bed": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_double, *_err]),
+    "wl_set_manning": (C.c_int, [C.c_void_p, _dp, C.c_size_t, *_err]),
+    "wl_set_source": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_uint32, C.c_int, *_err]),
+    "wl_enqueue_steps": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32, C.c_float]),
+    "wl_run_steps": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, *_err]),
+    "wl_advance": (C.c_uint64, [C.c_void_p, C.c_double, *_err]),
+    "wl_state_hash": (C.c_uint64, [C.c_void_p, *_err]),
+    "wl_read_partials_bits": (C.c_int, [C.c_void_p, C.POINTER(Partial), C.c_size_t, *_err]),
+    "wl_read_ledger_bits": (C.c_int, [C.c_void_p, C.POINTER(LedgerBits), *_err]),
+    "wl_run_length_pass": (C.c_int, [C.c_void_p, C.c_float, *_err]),
+    "wl_hash_floats": (C.c_uint64, [_fp, C.c_size_t]),
+    "wl_step_stream": (wl_stream, [C.c_void_p]),
+    "wl_device_planes": (C.c_int, [C.c_void_p, C.POINTER(_fp), C.POINTER(_fp), *_err]),
+}
+
+
+def bind(lib: C.CDLL) -> C.CDLL:
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name, None)
+        if f is None:
+            continue  # a symbol check is the tests' job (tests/test_abi.py)
+        f.restype = res
+        f.argtypes = args
+    return lib

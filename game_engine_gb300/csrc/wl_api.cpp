@@ -1,0 +1,347 @@
+// The C ABI of include/wlcuda.h: water_live::DeviceStep's calls over a TileSet of one tile.
+// Each function names the reference call it stands in for (systems/water_live/src/water_live.cpp).
+#include "../../include/wlcuda.h"
+
+#include "wl_tiles.h"
+
+#include <cstddef>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+using wlc::TileSet;
+
+struct wl_step {
+  TileSet set;
+  wl_config config{};
+  wl_options options{};
+  uint32_t flags = 0;  // the reference's flags_ (water_live.h:239)
+  uint32_t source_every = 1;
+  uint32_t cells = 0;
+  uint32_t groups = 0;
+};
+
+// The mirrored structs keep the reference's sizes and offsets (water_live_tests.cpp:22-36,
+// size_table.cpp:8-10).
+static_assert(sizeof(wl_step_params) == 120, "StepParams is 120 bytes");
+static_assert(offsetof(wl_step_params, ledger) == 48, "");
+static_assert(offsetof(wl_step_params, nx) == 56, "");
+static_assert(offsetof(wl_step_params, flags) == 72, "");
+static_assert(offsetof(wl_step_params, max_dt) == 92, "");
+static_assert(offsetof(wl_step_params, source_scale) == 96, "");
+static_assert(offsetof(wl_step_params, faces_x) == 104, "");
+static_assert(offsetof(wl_step_params, faces_y) == 112, "");
+static_assert(sizeof(wl_partial) == 32 && offsetof(wl_partial, roundoff_m3) == 16, "");
+static_assert(sizeof(wl_ledger_bits) == 48, "");
+static_assert(offsetof(wl_ledger_bits, remaining_s) == 32, "");
+static_assert(offsetof(wl_ledger_bits, dt) == 36, "");
+static_assert(offsetof(wl_ledger_bits, steps) == 40, "");
+static_assert(sizeof(wl_partial) == sizeof(wlc::Partial), "");
+static_assert(sizeof(wl_ledger_bits) == sizeof(wlc::LedgerBits), "");
+
+namespace {
+
+int fail(char* err, size_t len, int code, const std::string& msg) {
+  if (err != nullptr && len > 0) {
+    const size_t k = msg.size() < len - 1 ? msg.size() : len - 1;
+    std::memcpy(err, msg.data(), k);
+    err[k] = '\0';
+  }
+  return code;
+}
+
+int cuda_fail(char* err, size_t len, const std::string& msg) {
+  const int code = msg.find("wait limit") != std::string::npos ? WL_ERR_TIMEOUT : WL_ERR_CUDA;
+  return fail(err, len, code, msg);
+}
+
+bool valid(const wl_step* s) { return s != nullptr && s->set.valid(); }
+
+const char* k_no_device = "water_live: no device";
+
+int flush(wl_step* s, wl_ledger_bits* bits, std::string* msg) {
+  if (!s->set.length_pass(0, 0.0f, msg)) return WL_ERR_CUDA;
+  wlc::TileCtl c;
+  if (!s->set.read_ctl(0, c, msg)) return WL_ERR_CUDA;
+  std::memcpy(bits, &c.ledger, sizeof *bits);
+  return WL_OK;
+}
+
+void widen(const wl_ledger_bits& l, wl_ledger* out) {  // water_live.cpp:374-379
+  out->source_m3 = double(l.source_hi) + double(l.source_lo);
+  out->open_edge_out_m3 = double(l.open_hi) + double(l.open_lo);
+  out->roundoff_m3 = double(l.roundoff_hi) + double(l.roundoff_lo);
+  out->time_s = double(l.time_hi) + double(l.time_lo);
+  out->remaining_s = double(l.remaining_s);
+  out->steps = l.steps;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wl_create(const wl_config* config, const wl_options* options, wl_step** out, char* err,
+              size_t err_len) {
+  if (out == nullptr || config == nullptr)
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no config");
+  *out = nullptr;
+  if (config->nx == 0 || config->ny == 0)  // water_live.cpp:108
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: an empty grid");
+  auto* s = new (std::nothrow) wl_step;
+  if (s == nullptr) return fail(err, err_len, WL_ERR_ALLOC, "water_live: out of host memory");
+  s->config = *config;
+  if (options != nullptr) s->options = *options;
+  wlc::TileSpec t;
+  t.nx = config->nx;
+  t.ny = config->ny;
+  t.cell_m = config->cell_m;
+  t.gravity = config->gravity;
+  t.cfl = config->cfl;
+  t.dry_depth_m = config->dry_depth_m;
+  s->flags = 0;
+  if (config->west_open) s->flags |= WL_FLAG_WEST_OPEN;
+  if (config->east_open) s->flags |= WL_FLAG_EAST_OPEN;
+  if (config->south_open) s->flags |= WL_FLAG_SOUTH_OPEN;
+  if (config->north_open) s->flags |= WL_FLAG_NORTH_OPEN;
+  if (s->options.stored_faces) s->flags |= WL_FLAG_STORED_FACES;
+  t.open_edges = s->flags & 15u;
+  std::string msg;
+  if (!s->set.create(config->device, {t}, s->options.ops == WL_OPS_FIXED,
+                     wlc::BlockShape::k32x32, {}, &msg)) {
+    delete s;
+    return cuda_fail(err, err_len, msg);
+  }
+  s->cells = config->nx * config->ny;
+  s->groups = ((config->nx + 15) / 16) * ((config->ny + 15) / 16);
+  *out = s;
+  return WL_OK;
+}
+
+void wl_destroy(wl_step* step) { delete step; }
+
+int wl_valid(const wl_step* step) { return valid(step) ? 1 : 0; }
+
+uint32_t wl_cell_count(const wl_step* step) { return valid(step) ? step->cells : 0u; }
+
+uint32_t wl_group_count(const wl_step* step) { return valid(step) ? step->groups : 0u; }
+
+int wl_write_state(wl_step* s, const double* h, const double* hu, const double* hv, size_t n,
+                   char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (n != s->cells || h == nullptr || hu == nullptr || hv == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a state that does not fit the grid");
+  std::string msg;
+  if (!s->set.write_state(0, h, hu, hv, &msg) || !s->set.prime(&msg))
+    return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_read_state(wl_step* s, double* h, double* hu, double* hv, size_t n, char* err,
+                  size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (n != s->cells || h == nullptr || hu == nullptr || hv == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a state that does not fit the grid");
+  std::string msg;
+  if (!s->set.read_state(0, h, hu, hv, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_read_state_bits(wl_step* s, float* planes, size_t count, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (planes == nullptr || count != size_t(WL_STATE_PLANES) * s->cells)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: planes of the wrong size");
+  std::string msg;
+  if (!s->set.read_state_bits(0, planes, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_read_ledger(wl_step* s, wl_ledger* out, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no ledger");
+  wl_ledger_bits l;
+  std::string msg;
+  if (flush(s, &l, &msg) != WL_OK) return cuda_fail(err, err_len, msg);
+  widen(l, out);
+  return WL_OK;
+}
+
+int wl_set_bed(wl_step* s, const double* bed, size_t n, double datum, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (n != s->cells || bed == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a bed that does not fit the grid");
+  std::string msg;
+  if (!s->set.set_plane(0, 0, bed, datum, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_set_manning(wl_step* s, const double* manning, size_t n, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  std::string msg;
+  if (n == 0) {
+    s->flags &= ~WL_FLAG_MANNING;
+    if (!s->set.set_flags(0, s->flags, s->source_every, false, &msg))
+      return cuda_fail(err, err_len, msg);
+    return WL_OK;
+  }
+  if (n != s->cells || manning == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a Manning's n that does not fit");
+  if (!s->set.set_plane(0, 1, manning, 0.0, &msg)) return cuda_fail(err, err_len, msg);
+  s->flags |= WL_FLAG_MANNING;
+  if (!s->set.set_flags(0, s->flags, s->source_every, false, &msg))
+    return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_set_source(wl_step* s, const double* source, size_t n, uint32_t every, int compensate,
+                  char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  // water_live.cpp:465-486: the clock and the compensation change even when the source is refused.
+  s->source_every = every == 0 ? 1 : every;
+  if (compensate) s->flags |= WL_FLAG_COMPENSATE;
+  else s->flags &= ~WL_FLAG_COMPENSATE;
+  std::string msg;
+  if (n == 0) {
+    s->flags &= ~WL_FLAG_SOURCE;
+    if (!s->set.set_flags(0, s->flags, s->source_every, true, &msg))
+      return cuda_fail(err, err_len, msg);
+    return WL_OK;
+  }
+  if (n != s->cells || source == nullptr) {
+    if (!s->set.set_flags(0, s->flags, s->source_every, true, &msg))
+      return cuda_fail(err, err_len, msg);
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a source that does not fit");
+  }
+  if (!s->set.set_plane(0, 2, source, 0.0, &msg)) return cuda_fail(err, err_len, msg);
+  s->flags |= WL_FLAG_SOURCE;
+  if (!s->set.set_flags(0, s->flags, s->source_every, true, &msg))
+    return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_enqueue_steps(wl_step* s, wl_stream stream, uint32_t count, float max_dt) {
+  if (!valid(s)) return WL_ERR_INVALID;
+  cudaStream_t st = stream == nullptr ? s->set.stream() : reinterpret_cast<cudaStream_t>(stream);
+  if (cudaSetDevice(s->set.device()) != cudaSuccess) return WL_ERR_CUDA;
+  return s->set.enqueue_ticks(st, count, max_dt) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
+}
+
+int wl_run_steps(wl_step* s, uint32_t count, float max_dt, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (cudaSetDevice(s->set.device()) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
+  const cudaError_t e = s->set.enqueue_ticks(s->set.stream(), count, max_dt);
+  if (e != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, std::string("water_live: the tick: ") + cudaGetErrorString(e));
+  std::string msg;
+  if (!s->set.wait(&msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+uint64_t wl_advance(wl_step* s, double duration_s, char* err, size_t err_len) {
+  if (!valid(s)) {
+    fail(err, err_len, WL_ERR_INVALID, k_no_device);
+    return 0;
+  }
+  if (!(duration_s > 0.0)) return 0;
+  // water_live.cpp:600-606: a coarser source clock counts steps on the host; refused.
+  if ((s->flags & WL_FLAG_SOURCE) != 0u && s->source_every > 1) {
+    fail(err, err_len, WL_ERR_REFUSED,
+         "water_live: advance refuses a source on a coarser clock (set_source every > 1)");
+    return 0;
+  }
+  constexpr uint32_t k_batch = 64;
+  constexpr uint32_t k_most_batches = 1u << 16;
+  std::string msg;
+  wl_ledger_bits start, now, end;
+  if (flush(s, &start, &msg) != WL_OK ||
+      !s->set.set_remaining(0, static_cast<float>(duration_s), &msg)) {
+    cuda_fail(err, err_len, msg);
+    return 0;
+  }
+  const float inf = std::numeric_limits<float>::infinity();
+  bool done = false;
+  for (uint32_t batch = 0; batch < k_most_batches && !done; ++batch) {
+    if (s->set.enqueue_ticks(s->set.stream(), k_batch, inf) != cudaSuccess) {
+      fail(err, err_len, WL_ERR_CUDA, "water_live: the tick");
+      return 0;
+    }
+    if (flush(s, &now, &msg) != WL_OK) {
+      cuda_fail(err, err_len, msg);
+      return 0;
+    }
+    done = !(double(now.remaining_s) > 0.0);
+  }
+  if (flush(s, &end, &msg) != WL_OK || !s->set.set_remaining(0, inf, &msg)) {
+    cuda_fail(err, err_len, msg);
+    return 0;
+  }
+  if (!done) {
+    fail(err, err_len, WL_ERR_UNFINISHED, "water_live: the advance did not finish");
+    return 0;
+  }
+  return uint64_t(end.steps) - uint64_t(start.steps);
+}
+
+uint64_t wl_state_hash(wl_step* s, char* err, size_t err_len) {
+  if (!valid(s)) {
+    fail(err, err_len, WL_ERR_INVALID, k_no_device);
+    return 0;
+  }
+  std::vector<float> planes(size_t(WL_STATE_PLANES) * s->cells);
+  std::string msg;
+  if (!s->set.read_state_bits(0, planes.data(), &msg)) {
+    cuda_fail(err, err_len, msg);
+    return 0;
+  }
+  return wlc::fnv1a_floats(planes.data(), planes.size());
+}
+
+int wl_read_partials_bits(wl_step* s, wl_partial* out, size_t count, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (out == nullptr || count != s->groups)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: records of the wrong count");
+  std::string msg;
+  if (!s->set.read_partials(0, reinterpret_cast<wlc::Partial*>(out), &msg))
+    return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_read_ledger_bits(wl_step* s, wl_ledger_bits* out, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no ledger");
+  wlc::TileCtl c;
+  std::string msg;
+  if (!s->set.read_ctl(0, c, &msg)) return cuda_fail(err, err_len, msg);
+  std::memcpy(out, &c.ledger, sizeof *out);
+  return WL_OK;
+}
+
+int wl_run_length_pass(wl_step* s, float max_dt, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  std::string msg;
+  if (!s->set.length_pass(0, max_dt, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+uint64_t wl_hash_floats(const float* values, size_t count) {
+  if (values == nullptr) count = 0;
+  return wlc::fnv1a_floats(values, count);
+}
+
+wl_stream wl_step_stream(wl_step* s) {
+  return valid(s) ? reinterpret_cast<wl_stream>(s->set.stream()) : nullptr;
+}
+
+int wl_device_planes(wl_step* s, float** planes, float** bed, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  wlc::TileCtl c;
+  std::string msg;
+  if (!s->set.read_ctl(0, c, &msg)) return cuda_fail(err, err_len, msg);
+  if (planes) *planes = s->set.device_state(0, c.cur & 1u);
+  if (bed) *bed = const_cast<float*>(s->set.desc(0).bed);
+  return WL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,259 @@
+// Device-side arithmetic and layout of the live-water tick (sm_103a).
+//
+// The scheme is the reference's (systems/water_live/shaders/water_step.slang, and its FP64 twin
+// domain/water_state/src/water_state.cpp): the hydrostatic reconstruction over the central-upwind
+// flux on h, hu, hv. Every expression below keeps the reference's operand order. The translation
+// unit is compiled with --fmad=false -prec-div=true -prec-sqrt=true -ftz=false, and division and
+// square root are spelled with the _rn intrinsics, so each + - * / sqrt is one correctly rounded
+// IEEE operation whatever the flags, and the bytes equal the CPU restatement's.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wlc {
+
+constexpr uint32_t kFlagWestOpen = 1u;  // water_live.h:90-97
+constexpr uint32_t kFlagEastOpen = 2u;
+constexpr uint32_t kFlagSouthOpen = 4u;
+constexpr uint32_t kFlagNorthOpen = 8u;
+constexpr uint32_t kFlagManning = 16u;
+constexpr uint32_t kFlagSource = 32u;
+constexpr uint32_t kFlagCompensate = 64u;
+constexpr uint32_t kFlagStoredFaces = 128u;
+constexpr uint32_t kGroupSide = 16u;
+constexpr uint32_t kGroupCells = 256u;
+constexpr uint32_t kStatePlanes = 4u;
+constexpr int kThreads = 256;  // one CTA: 8 warps; also the length pass's 256 lanes
+
+// water_live::WaterPartial (water_live.h:114-121).
+struct Partial {
+  float speed_x, speed_y, source_m3, open_m3, roundoff_m3, pad0, pad1, pad2;
+};
+static_assert(sizeof(Partial) == 32, "WaterPartial is 32 bytes");
+
+// water_live::WaterLedger (water_live.h:124-137).
+struct LedgerBits {
+  float time_hi, time_lo, source_hi, source_lo, open_hi, open_lo, roundoff_hi, roundoff_lo;
+  float remaining_s, dt;
+  uint32_t steps, pad;
+};
+static_assert(sizeof(LedgerBits) == 48, "WaterLedger is 48 bytes");
+
+// A tile's control block, all of a tick's state that is not a plane: the ledger as the reference
+// keeps it, which copy holds the state, which record buffer holds the last update's records, the
+// last update's largest speeds (the next step's length is chosen from them), and the source's
+// clock. Every launch reads it and the tile's last work item rewrites it, so a captured graph of
+// ticks replays correctly any number of times.
+struct TileCtl {
+  LedgerBits ledger;       // 0: the ledger (read_ledger_bits copies these 48 bytes)
+  LedgerBits ledger_next;  // 48: this tick's ledger, committed by the tile's last work item
+  uint32_t cur;            // 96: the copy that holds the state
+  uint32_t rec;            // 100: the record buffer that holds the last update's records
+  uint32_t prev_a;         // 104: largest |u| + c of the last update (float bits, never -0)
+  uint32_t prev_b;         // 108: largest |v| + c
+  uint32_t max_a;          // 112: this tick's running maxima (atomicMax on the bits)
+  uint32_t max_b;          // 116
+  uint32_t done;           // 120: work items of this tile finished in this launch
+  uint32_t src_phase;      // 124: steps since the source last applied (set_source's clock)
+  uint32_t error;          // 128: a device error word (0: none)
+  uint32_t ticks;          // 132: launches that stepped this tile (a diagnosis counter)
+  uint32_t pad[2];
+};
+static_assert(sizeof(TileCtl) == 144, "TileCtl layout");
+
+// One rectangle of water as the kernels see it. The planes are the reference's layout: a copy is
+// four planes of nx * ny floats (h, hu, hv, remainder), cell (x, y) at y * nx + x.
+struct TileDesc {
+  float* state[2];
+  const float* bed;
+  const float* manning;
+  const float* source;
+  Partial* rec[2];
+  TileCtl* ctl;
+  uint32_t nx, ny, groups_x, groups_y;
+  uint32_t flags;         // kFlag* for this tile (edges, Manning, source, compensate)
+  uint32_t source_every;  // set_source's clock
+  float cell_m, gravity, cfl, dry;
+  uint32_t blocks_x, blocks_y;  // work items: blocks of the launch's block shape
+  uint32_t item_base, items;
+};
+
+// A launch's dynamic work counter: CTAs take work items in order; the last CTA to leave resets it.
+struct WorkCtl {
+  uint32_t next;
+  uint32_t exited;
+  uint32_t pad[2];
+};
+
+// ---- the arithmetic (water_step.slang:105-191) -------------------------------------------------
+
+__device__ __forceinline__ float max2(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float min2(float a, float b) { return a < b ? a : b; }
+
+// rcp_fixed (slang:112-124).
+__device__ __forceinline__ float rcp_fixed(float x) {
+  const uint32_t bits = __float_as_uint(x);
+  if (bits >= 0x7e800000u) return 0.0f;
+  if (bits < 0x00800000u) return __uint_as_float(0x7f7fffffu);
+  float r = __uint_as_float(0x7ef311c3u - bits);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float t = __fmul_rn(x, r);
+    const float e = __fsub_rn(2.0f, t);
+    r = __fmul_rn(r, e);
+  }
+  return r;
+}
+
+// rsqrt_fixed (slang:128-139).
+__device__ __forceinline__ float rsqrt_fixed(float x) {
+  float y = __uint_as_float(0x5f375a86u - (__float_as_uint(x) >> 1));
+  const float half_x = __fmul_rn(0.5f, x);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float yy = __fmul_rn(y, y);
+    const float t = __fmul_rn(half_x, yy);
+    const float e = __fsub_rn(1.5f, t);
+    y = __fmul_rn(y, e);
+  }
+  return y;
+}
+
+// cbrt_fixed (slang:143-154); 1.0 / 3.0 folds to the float nearest a third.
+__device__ __forceinline__ float cbrt_fixed(float h) {
+  float x = __uint_as_float(__float_as_uint(h) / 3u + 709921077u);
+  const float third = 0.333333343267f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float xx = __fmul_rn(x, x);
+    const float q = __fmul_rn(h, rcp_fixed(xx));
+    const float twice = __fadd_rn(x, x);
+    const float s = __fadd_rn(twice, q);
+    x = __fmul_rn(s, third);
+  }
+  return x;
+}
+
+// The two forms of the arithmetic (water_live.h:57-62). Native: IEEE division and square root.
+// Both forms take the cube root from the fixed construction (the shader's native log2/exp2 is not
+// reproducible on any two devices, nor against a CPU).
+template <bool FIXED>
+struct Ops {
+  static __device__ __forceinline__ float div(float a, float b) {
+    if (FIXED) {
+      if (a == 0.0f) return a;
+      return __fmul_rn(a, rcp_fixed(b));
+    }
+    return __fdiv_rn(a, b);
+  }
+  static __device__ __forceinline__ float sqrt(float x) {
+    if (FIXED) {
+      if (__float_as_uint(x) < 0x00800000u) return 0.0f;
+      return __fmul_rn(x, rsqrt_fixed(x));
+    }
+    return __fsqrt_rn(x);
+  }
+  static __device__ __forceinline__ float cbrt(float h) { return cbrt_fixed(h); }
+};
+
+// pressure (slang:186-191): (0.5 g) h h.
+__device__ __forceinline__ float pressure(float half_g, float h) {
+  return __fmul_rn(__fmul_rn(half_g, h), h);
+}
+
+// face (slang:274-292) over face_flux (slang:204-262): the face's bed the larger of the two, each
+// side reconstructed against it, the central-upwind flux between them, and the normal momentum's
+// flux less each side's pressure. Returns {h, nl, nr, t}.
+template <bool FIXED>
+__device__ __forceinline__ float4 face(float g, float half_g, float hl0, float zl, float ul,
+                                       float vl, float hr0, float zr, float ur, float vr) {
+  using O = Ops<FIXED>;
+  const float zf = max2(zl, zr);
+  const float el = __fsub_rn(__fadd_rn(hl0, zl), zf);
+  const float er = __fsub_rn(__fadd_rn(hr0, zr), zf);
+  const float hl = el > 0.0f ? el : 0.0f;
+  const float hr = er > 0.0f ? er : 0.0f;
+  const float pl = pressure(half_g, hl);
+  const float pr = pressure(half_g, hr);
+  float fh, fn, ft;
+  if (hl == hr && ul == ur && vl == vr) {
+    const float q = __fmul_rn(hl, ul);
+    fh = q;
+    fn = __fadd_rn(__fmul_rn(q, ul), pl);
+    ft = __fmul_rn(q, vl);
+  } else {
+    const float cl = O::sqrt(__fmul_rn(g, hl));
+    const float cr = O::sqrt(__fmul_rn(g, hr));
+    const float ap = max2(max2(__fadd_rn(ur, cr), __fadd_rn(ul, cl)), 0.0f);
+    const float am = min2(min2(__fsub_rn(ur, cr), __fsub_rn(ul, cl)), 0.0f);
+    const float span = __fsub_rn(ap, am);
+    if (!(span > 0.0f)) {
+      fh = 0.0f;
+      fn = 0.0f;
+      ft = 0.0f;
+    } else {
+      const float ql = __fmul_rn(hl, ul);
+      const float qr = __fmul_rn(hr, ur);
+      const float apam = __fmul_rn(ap, am);
+      const float h6 = __fadd_rn(__fsub_rn(__fmul_rn(ap, ql), __fmul_rn(am, qr)),
+                                 __fmul_rn(apam, __fsub_rn(hr, hl)));
+      const float n2 = __fadd_rn(__fmul_rn(ql, ul), pl);
+      const float n5 = __fadd_rn(__fmul_rn(qr, ur), pr);
+      const float n10 = __fadd_rn(__fsub_rn(__fmul_rn(ap, n2), __fmul_rn(am, n5)),
+                                  __fmul_rn(apam, __fsub_rn(qr, ql)));
+      const float t7 = __fsub_rn(__fmul_rn(hr, vr), __fmul_rn(hl, vl));
+      const float t10 = __fadd_rn(__fsub_rn(__fmul_rn(ap, __fmul_rn(ql, vl)),
+                                            __fmul_rn(am, __fmul_rn(qr, vr))),
+                                  __fmul_rn(apam, t7));
+      fh = O::div(h6, span);
+      fn = O::div(n10, span);
+      ft = O::div(t10, span);
+    }
+  }
+  return make_float4(fh, __fsub_rn(fn, pl), __fsub_rn(fn, pr), ft);
+}
+
+// |u| + c and |v| + c (slang:317-326).
+template <bool FIXED>
+__device__ __forceinline__ void cell_speeds(float g, float dry, float h, float hu, float hv,
+                                            float& ax, float& ay) {
+  using O = Ops<FIXED>;
+  const bool wet = h >= dry;
+  const float u = wet ? O::div(hu, h) : 0.0f;
+  const float v = wet ? O::div(hv, h) : 0.0f;
+  const float c = O::sqrt(__fmul_rn(g, h));
+  ax = __fadd_rn(fabsf(u), c);
+  ay = __fadd_rn(fabsf(v), c);
+}
+
+// pair_add (slang:391-404): TwoSum, then Fast2Sum.
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float sa = __fsub_rn(s, bb);
+  const float da = __fsub_rn(hi, sa);
+  const float db = __fsub_rn(x, bb);
+  const float e = __fadd_rn(da, db);
+  const float l = __fadd_rn(lo, e);
+  const float h2 = __fadd_rn(s, l);
+  const float back = __fsub_rn(h2, s);
+  const float l2 = __fsub_rn(l, back);
+  hi = h2;
+  lo = l2;
+}
+
+// The step's length (slang:464-474) from the last update's largest speeds and the time left.
+template <bool FIXED>
+__device__ __forceinline__ float choose_dt(float a, float b, float cfl, float cell_m,
+                                           float max_dt, float remaining) {
+  if (!(max_dt > 0.0f)) return 0.0f;
+  const float speed = __fadd_rn(a, b);
+  const float reach = __fmul_rn(cfl, cell_m);
+  const float stable = speed > 0.0f ? Ops<FIXED>::div(reach, speed) : __int_as_float(0x7f800000);
+  float dt = min2(stable, max_dt);
+  dt = min2(dt, remaining);
+  return dt;
+}
+
+}  // namespace wlc

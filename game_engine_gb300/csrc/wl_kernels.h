@@ -1,0 +1,47 @@
+// Host-side entry points of the tick's kernels (wl_kernels.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wlc {
+
+struct TileDesc;
+struct WorkCtl;
+
+// A tick launch: the tiles, which tile each work item belongs to (null: all items of tile 0), the
+// launch's work counter and the step's max_dt.
+struct TickArgs {
+  const TileDesc* tiles;
+  const uint32_t* item_tile;
+  WorkCtl* work;
+  uint32_t n_items;
+  float max_dt;
+};
+
+// The block of cells one work item steps. 32 x 32 is the default; the batched form's autotuner
+// chooses among all three.
+enum class BlockShape : uint8_t { k32x16 = 0, k32x32 = 1, k64x32 = 2 };
+
+size_t tick_smem_bytes(BlockShape shape);
+void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by);
+// Sets the kernels' shared-memory opt-in on the current device and returns the resident CTAs per
+// SM (0 on an error).
+int tick_occupancy(BlockShape shape, bool fixed, bool manning);
+
+cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickArgs& a, int grid,
+                        cudaStream_t s);
+// The records of the states just written (one CTA a work item, the same items as the tick's).
+cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaStream_t s);
+cudaError_t launch_length_pass(bool fixed, const TileDesc* tiles, uint32_t tile, float max_dt,
+                               cudaStream_t s);
+cudaError_t launch_write_state(TileDesc* tiles, uint32_t tile, size_t n, const double* h,
+                               const double* hu, const double* hv, cudaStream_t s);
+cudaError_t launch_plane(float* dst, const double* src, size_t n, double datum, cudaStream_t s);
+cudaError_t launch_read_state(const TileDesc* tiles, uint32_t tile, size_t n, double* h,
+                              double* hu, double* hv, cudaStream_t s);
+cudaError_t launch_copy_state(const TileDesc* tiles, uint32_t tile, size_t n, float* dst,
+                              cudaStream_t s);
+
+}  // namespace wlc

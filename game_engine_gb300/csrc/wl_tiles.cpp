@@ -1,0 +1,485 @@
+// A set of water tiles on one device (wl_tiles.h).
+#include "wl_tiles.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <thread>
+
+namespace wlc {
+
+namespace {
+
+constexpr size_t kAlign = 256;
+
+size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+double wait_limit_s() {
+  const char* e = std::getenv("WLCUDA_WAIT_S");
+  if (e != nullptr) {
+    const double v = std::atof(e);
+    if (v > 0.0) return v;
+  }
+  return 300.0;
+}
+
+}  // namespace
+
+uint64_t fnv1a_floats(const float* v, size_t n, uint64_t hash) {
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t bits;
+    std::memcpy(&bits, v + i, 4);
+    for (uint32_t b = 0; b < 4; ++b) {
+      hash ^= (bits >> (8 * b)) & 0xffu;
+      hash *= 0x100000001b3ull;
+    }
+  }
+  return hash;
+}
+
+cudaError_t wait_stream(cudaStream_t s, bool* timed_out) {
+  if (timed_out) *timed_out = false;
+  const auto start = std::chrono::steady_clock::now();
+  const double limit = wait_limit_s();
+  for (uint32_t spin = 0;; ++spin) {
+    const cudaError_t e = cudaStreamQuery(s);
+    if (e != cudaErrorNotReady) return e;
+    const double waited =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+    if (waited > limit) {
+      if (timed_out) *timed_out = true;
+      return cudaErrorNotReady;
+    }
+    if (spin > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+TileSet::~TileSet() { destroy(); }
+
+bool TileSet::check(cudaError_t e, std::string* err, const char* what) {
+  if (e == cudaSuccess) return true;
+  if (err) *err = std::string("water_live: ") + what + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+void TileSet::destroy() {
+  if (device_ >= 0) cudaSetDevice(device_);
+  if (stream_ != nullptr) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+  if (base_ != nullptr) cudaFree(base_);
+  if (staging_ != nullptr) cudaFree(staging_);
+  stream_ = nullptr;
+  base_ = nullptr;
+  staging_ = nullptr;
+  staging_bytes_ = 0;
+  host_.clear();
+  d_desc_ = nullptr;
+  d_ctl_ = nullptr;
+  d_work_ = nullptr;
+  d_item_tile_ = nullptr;
+  n_items_ = 0;
+  device_ = -1;
+}
+
+bool TileSet::any_manning() const {
+  for (const TileDesc& d : host_)
+    if (d.flags & kFlagManning) return true;
+  return false;
+}
+
+bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_ops,
+                     BlockShape shape, const std::vector<uint32_t>& order, std::string* err) {
+  destroy();
+  if (tiles.empty()) {
+    if (err) *err = "water_live: no tiles";
+    return false;
+  }
+  for (const TileSpec& t : tiles) {
+    if (t.nx == 0 || t.ny == 0) {
+      if (err) *err = "water_live: an empty grid";
+      return false;
+    }
+    if (uint64_t(t.nx) * t.ny >= (1ull << 31)) {
+      if (err) *err = "water_live: a grid of 2^31 cells or more";
+      return false;
+    }
+  }
+  if (!check(cudaSetDevice(device), err, "cudaSetDevice")) return false;
+  device_ = device;
+  fixed_ = fixed_ops;
+  if (!check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), err, "cudaStreamCreate")) {
+    destroy();
+    return false;
+  }
+  // One allocation: per tile the planes and records, then the control blocks and descriptors.
+  const size_t nt = tiles.size();
+  std::vector<size_t> off_state(nt), off_inputs(nt), off_rec(nt);
+  size_t total = 0;
+  total_cells_ = 0;
+  for (size_t i = 0; i < nt; ++i) {
+    const size_t n = size_t(tiles[i].nx) * tiles[i].ny;
+    const size_t groups = size_t((tiles[i].nx + 15) / 16) * ((tiles[i].ny + 15) / 16);
+    total_cells_ += n;
+    off_state[i] = total;
+    total += 2 * align_up(kStatePlanes * n * sizeof(float));
+    off_inputs[i] = total;
+    total += 3 * align_up(n * sizeof(float));
+    off_rec[i] = total;
+    total += 2 * align_up(groups * sizeof(Partial));
+  }
+  const size_t off_ctl = total;
+  total += align_up(nt * sizeof(TileCtl));
+  const size_t off_desc = total;
+  total += align_up(nt * sizeof(TileDesc));
+  const size_t off_work = total;
+  total += align_up(sizeof(WorkCtl));
+  if (!check(cudaMalloc(&base_, total), err, "cudaMalloc")) {
+    base_ = nullptr;
+    destroy();
+    return false;
+  }
+  bytes_ = total;
+  if (!check(cudaMemsetAsync(base_, 0, total, stream_), err, "cudaMemset")) {
+    destroy();
+    return false;
+  }
+  d_ctl_ = reinterpret_cast<TileCtl*>(base_ + off_ctl);
+  d_desc_ = reinterpret_cast<TileDesc*>(base_ + off_desc);
+  d_work_ = reinterpret_cast<WorkCtl*>(base_ + off_work);
+  host_.resize(nt);
+  for (size_t i = 0; i < nt; ++i) {
+    const TileSpec& t = tiles[i];
+    const size_t n = size_t(t.nx) * t.ny;
+    const size_t groups = size_t((t.nx + 15) / 16) * ((t.ny + 15) / 16);
+    TileDesc& d = host_[i];
+    std::memset(&d, 0, sizeof d);
+    const size_t plane_bytes = align_up(kStatePlanes * n * sizeof(float));
+    d.state[0] = reinterpret_cast<float*>(base_ + off_state[i]);
+    d.state[1] = reinterpret_cast<float*>(base_ + off_state[i] + plane_bytes);
+    const size_t in_bytes = align_up(n * sizeof(float));
+    d.bed = reinterpret_cast<const float*>(base_ + off_inputs[i]);
+    d.manning = reinterpret_cast<const float*>(base_ + off_inputs[i] + in_bytes);
+    d.source = reinterpret_cast<const float*>(base_ + off_inputs[i] + 2 * in_bytes);
+    const size_t rec_bytes = align_up(groups * sizeof(Partial));
+    d.rec[0] = reinterpret_cast<Partial*>(base_ + off_rec[i]);
+    d.rec[1] = reinterpret_cast<Partial*>(base_ + off_rec[i] + rec_bytes);
+    d.ctl = d_ctl_ + i;
+    d.nx = t.nx;
+    d.ny = t.ny;
+    d.groups_x = (t.nx + 15) / 16;
+    d.groups_y = (t.ny + 15) / 16;
+    d.flags = t.open_edges & 15u;
+    d.source_every = 1;
+    // The kernels' constants round like the reference's push constants (water_live.cpp:245-248).
+    d.cell_m = static_cast<float>(t.cell_m);
+    d.gravity = static_cast<float>(t.gravity);
+    d.cfl = static_cast<float>(t.cfl);
+    d.dry = static_cast<float>(t.dry_depth_m);
+  }
+  // Empty ledgers: every field zero but the time left, +inf between advances.
+  std::vector<TileCtl> ctl(nt);
+  for (TileCtl& c : ctl) {
+    std::memset(&c, 0, sizeof c);
+    c.ledger.remaining_s = std::numeric_limits<float>::infinity();
+  }
+  if (!check(cudaMemcpyAsync(d_ctl_, ctl.data(), nt * sizeof(TileCtl), cudaMemcpyHostToDevice,
+                             stream_),
+             err, "upload of the ledgers") ||
+      !check(cudaStreamSynchronize(stream_), err, "cudaStreamSynchronize")) {
+    destroy();
+    return false;
+  }
+  for (BlockShape s : {BlockShape::k32x16, BlockShape::k32x32, BlockShape::k64x32})
+    for (bool m : {false, true})
+      if (tick_occupancy(s, fixed_, m) <= 0) {
+        if (err) *err = "water_live: the tick kernel cannot be resident on this device";
+        destroy();
+        return false;
+      }
+  if (!layout_items(shape, order, err)) {
+    destroy();
+    return false;
+  }
+  return prime(err);
+}
+
+bool TileSet::layout_items(BlockShape shape, const std::vector<uint32_t>& order,
+                           std::string* err) {
+  uint32_t bx = 0, by = 0;
+  block_dims(shape, bx, by);
+  const uint32_t nt = tile_count();
+  order_ = order;
+  if (order_.size() != nt) {
+    order_.resize(nt);
+    for (uint32_t i = 0; i < nt; ++i) order_[i] = i;
+  }
+  std::vector<uint32_t> item_tile;
+  uint64_t items = 0;
+  for (uint32_t k = 0; k < nt; ++k) {
+    TileDesc& d = host_[order_[k]];
+    d.blocks_x = (d.nx + bx - 1) / bx;
+    d.blocks_y = (d.ny + by - 1) / by;
+    d.items = d.blocks_x * d.blocks_y;
+    d.item_base = uint32_t(items);
+    items += d.items;
+  }
+  if (items >= (1ull << 32)) {
+    if (err) *err = "water_live: too many work items";
+    return false;
+  }
+  n_items_ = uint32_t(items);
+  if (nt > 1) {
+    item_tile.resize(n_items_);
+    for (uint32_t k = 0; k < nt; ++k) {
+      const TileDesc& d = host_[order_[k]];
+      std::fill(item_tile.begin() + d.item_base, item_tile.begin() + d.item_base + d.items,
+                order_[k]);
+    }
+  }
+  shape_ = shape;
+  int sms = 0;
+  if (!check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), err,
+             "cudaDeviceGetAttribute"))
+    return false;
+  const int occ = tick_occupancy(shape, fixed_, any_manning());
+  grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
+  // The items' tile indices: a separate small allocation, replaced on a reshape.
+  static_assert(sizeof(uint32_t) == 4, "");
+  if (d_item_tile_ != nullptr) {
+    cudaStreamSynchronize(stream_);
+    cudaFree(d_item_tile_);
+    d_item_tile_ = nullptr;
+  }
+  if (nt > 1) {
+    if (!check(cudaMalloc(&d_item_tile_, item_tile.size() * sizeof(uint32_t)), err, "cudaMalloc"))
+      return false;
+    if (!check(cudaMemcpyAsync(d_item_tile_, item_tile.data(), item_tile.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, stream_),
+               err, "upload of the work items"))
+      return false;
+  }
+  if (!check(cudaMemcpyAsync(d_desc_, host_.data(), nt * sizeof(TileDesc), cudaMemcpyHostToDevice,
+                             stream_),
+             err, "upload of the tiles"))
+    return false;
+  return check(cudaStreamSynchronize(stream_), err, "cudaStreamSynchronize");
+}
+
+bool TileSet::reshape(BlockShape shape, const std::vector<uint32_t>& order, std::string* err) {
+  if (!valid()) return false;
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(cudaStreamSynchronize(stream_), err, "cudaStreamSynchronize")) return false;
+  // The records are per 16 x 16 group whatever the block shape; only the items change.
+  return layout_items(shape, order, err);
+}
+
+bool TileSet::push_desc(uint32_t tile, std::string* err) {
+  if (!check(cudaMemcpyAsync(d_desc_ + tile, &host_[tile], sizeof(TileDesc),
+                             cudaMemcpyHostToDevice, stream_),
+             err, "upload of a tile"))
+    return false;
+  return check(cudaStreamSynchronize(stream_), err, "cudaStreamSynchronize");
+}
+
+cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt) {
+  TickArgs a;
+  a.tiles = d_desc_;
+  a.item_tile = d_item_tile_;
+  a.work = d_work_;
+  a.n_items = n_items_;
+  a.max_dt = max_dt;
+  const bool manning = any_manning();
+  for (uint32_t i = 0; i < count; ++i) {
+    const cudaError_t e = launch_tick(shape_, fixed_, manning, a, grid_, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t TileSet::enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt) {
+  TickArgs a;
+  a.tiles = d_desc_ + tile;
+  a.item_tile = nullptr;
+  a.work = d_work_;
+  a.n_items = host_[tile].items;
+  a.max_dt = max_dt;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
+  const bool manning = (host_[tile].flags & kFlagManning) != 0u;
+  const int occ = std::max(1, tick_occupancy(shape_, fixed_, manning));
+  const int grid = std::max(1, std::min<int>(int(a.n_items), sms * occ));
+  return launch_tick(shape_, fixed_, manning, a, grid, s);
+}
+
+cudaError_t TileSet::enqueue_prime(cudaStream_t s) {
+  TickArgs a;
+  a.tiles = d_desc_;
+  a.item_tile = d_item_tile_;
+  a.work = d_work_;
+  a.n_items = n_items_;
+  a.max_dt = 0.0f;
+  return launch_prime(shape_, fixed_, a, s);
+}
+
+cudaError_t TileSet::enqueue_length_pass(cudaStream_t s, uint32_t tile, float max_dt) {
+  return launch_length_pass(fixed_, d_desc_, tile, max_dt, s);
+}
+
+bool TileSet::wait(std::string* err) {
+  bool timed_out = false;
+  const cudaError_t e = wait_stream(stream_, &timed_out);
+  if (timed_out) {
+    if (err) *err = "water_live: the device did not finish within the wait limit";
+    return false;
+  }
+  return check(e, err, "the device");
+}
+
+bool TileSet::prime(std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(enqueue_prime(stream_), err, "the prime pass")) return false;
+  return wait(err);
+}
+
+bool TileSet::length_pass(uint32_t tile, float max_dt, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(enqueue_length_pass(stream_, tile, max_dt), err, "the length pass")) return false;
+  return wait(err);
+}
+
+bool TileSet::ensure_staging(size_t bytes, std::string* err) {
+  if (staging_bytes_ >= bytes) return true;
+  if (staging_ != nullptr) {
+    cudaStreamSynchronize(stream_);
+    cudaFree(staging_);
+    staging_ = nullptr;
+    staging_bytes_ = 0;
+  }
+  if (!check(cudaMalloc(&staging_, bytes), err, "cudaMalloc")) {
+    staging_ = nullptr;
+    return false;
+  }
+  staging_bytes_ = bytes;
+  return true;
+}
+
+bool TileSet::write_state(uint32_t tile, const double* h, const double* hu, const double* hv,
+                          std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = cells(tile);
+  if (!ensure_staging(3 * n * sizeof(double), err)) return false;
+  double* d = static_cast<double*>(staging_);
+  if (!check(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of the depth") ||
+      !check(cudaMemcpyAsync(d + n, hu, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of the momentum") ||
+      !check(cudaMemcpyAsync(d + 2 * n, hv, n * sizeof(double), cudaMemcpyHostToDevice, stream_),
+             err, "upload of the momentum") ||
+      !check(launch_write_state(d_desc_, tile, n, d, d + n, d + 2 * n, stream_), err,
+             "the state's conversion"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::set_plane(uint32_t tile, int which, const double* v, double datum,
+                        std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = cells(tile);
+  if (!ensure_staging(n * sizeof(double), err)) return false;
+  float* dst = nullptr;
+  const TileDesc& d = host_[tile];
+  if (which == 0) dst = const_cast<float*>(d.bed);
+  else if (which == 1) dst = const_cast<float*>(d.manning);
+  else dst = const_cast<float*>(d.source);
+  double* s = static_cast<double*>(staging_);
+  if (!check(cudaMemcpyAsync(s, v, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of an input") ||
+      !check(launch_plane(dst, s, n, datum, stream_), err, "an input's conversion"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::set_flags(uint32_t tile, uint32_t flags, uint32_t source_every, bool reset_phase,
+                        std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  host_[tile].flags = flags;
+  host_[tile].source_every = source_every;
+  if (reset_phase) {
+    if (!check(cudaMemsetAsync(&d_ctl_[tile].src_phase, 0, sizeof(uint32_t), stream_), err,
+               "cudaMemset"))
+      return false;
+  }
+  if (!push_desc(tile, err)) return false;
+  // The launch grid follows the variant the flags select.
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
+  const int occ = tick_occupancy(shape_, fixed_, any_manning());
+  grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
+  return true;
+}
+
+bool TileSet::set_remaining(uint32_t tile, float remaining, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(cudaMemcpyAsync(&d_ctl_[tile].ledger.remaining_s, &remaining, sizeof remaining,
+                             cudaMemcpyHostToDevice, stream_),
+             err, "upload of the time left"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::read_state(uint32_t tile, double* h, double* hu, double* hv, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = cells(tile);
+  if (!ensure_staging(3 * n * sizeof(double), err)) return false;
+  double* d = static_cast<double*>(staging_);
+  if (!check(launch_read_state(d_desc_, tile, n, d, d + n, d + 2 * n, stream_), err,
+             "the state's widening") ||
+      !check(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), err,
+             "read-back of the depth") ||
+      !check(cudaMemcpyAsync(hu, d + n, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), err,
+             "read-back of the momentum") ||
+      !check(cudaMemcpyAsync(hv, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+             err, "read-back of the momentum"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::read_state_bits(uint32_t tile, float* planes, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = cells(tile);
+  if (!ensure_staging(kStatePlanes * n * sizeof(float), err)) return false;
+  float* d = static_cast<float*>(staging_);
+  if (!check(launch_copy_state(d_desc_, tile, n, d, stream_), err, "the state's copy") ||
+      !check(cudaMemcpyAsync(planes, d, kStatePlanes * n * sizeof(float), cudaMemcpyDeviceToHost,
+                             stream_),
+             err, "read-back of the state"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::read_ctl(uint32_t tile, TileCtl& out, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(cudaMemcpyAsync(&out, d_ctl_ + tile, sizeof(TileCtl), cudaMemcpyDeviceToHost, stream_),
+             err, "read-back of the ledger"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::read_partials(uint32_t tile, Partial* out, std::string* err) {
+  TileCtl c;
+  if (!read_ctl(tile, c, err)) return false;
+  const TileDesc& d = host_[tile];
+  const size_t groups = size_t(d.groups_x) * d.groups_y;
+  if (!check(cudaMemcpyAsync(out, d.rec[c.rec & 1u], groups * sizeof(Partial),
+                             cudaMemcpyDeviceToHost, stream_),
+             err, "read-back of the records"))
+    return false;
+  return wait(err);
+}
+
+}  // namespace wlc

@@ -1,0 +1,108 @@
+// A set of water tiles on one device and the launches that step them (host side).
+//
+// The plain step (the reference's DeviceStep) is a set of one tile; the batched form is a set of
+// many. Every device buffer of a set lives in one allocation: per tile two copies of the four
+// state planes, the bed, Manning's n and the source, two record buffers; then the tiles'
+// control blocks and descriptors, the work items' tile indices and the launch's work counter.
+#pragma once
+
+#include "wl_device.cuh"
+#include "wl_kernels.h"
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace wlc {
+
+struct TileSpec {
+  uint32_t nx = 0, ny = 0;
+  double cell_m = 1.0, gravity = 9.81, cfl = 0.45, dry_depth_m = 1e-9;
+  uint32_t open_edges = 0;  // kFlag*Open bits
+};
+
+class TileSet {
+ public:
+  TileSet() = default;
+  ~TileSet();
+  TileSet(const TileSet&) = delete;
+  TileSet& operator=(const TileSet&) = delete;
+
+  // Allocates and clears every buffer (a dry state over a bed of zero, empty ledgers, records of
+  // that state). `order` lists the tiles in the order their work items are dealt (empty: by index).
+  bool create(int device, const std::vector<TileSpec>& tiles, bool fixed_ops, BlockShape shape,
+              const std::vector<uint32_t>& order, std::string* err);
+  void destroy();
+  bool valid() const { return base_ != nullptr; }
+
+  // The work items in another block shape (the autotuner's knob); the state is kept.
+  bool reshape(BlockShape shape, const std::vector<uint32_t>& order, std::string* err);
+
+  // ---- asynchronous, on `s` -----------------------------------------------------------------
+  cudaError_t enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt);
+  // One tile's own tick (the per-tile-launch form): only that tile's work items.
+  cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);
+  cudaError_t enqueue_prime(cudaStream_t s);
+  cudaError_t enqueue_length_pass(cudaStream_t s, uint32_t tile, float max_dt);
+
+  // ---- synchronous uploads and read-backs (each waits on the set's stream) -----------------
+  bool write_state(uint32_t tile, const double* h, const double* hu, const double* hv,
+                   std::string* err);
+  bool set_plane(uint32_t tile, int which, const double* v, double datum, std::string* err);
+  bool set_flags(uint32_t tile, uint32_t flags, uint32_t source_every, bool reset_phase,
+                 std::string* err);
+  bool set_remaining(uint32_t tile, float remaining, std::string* err);
+  bool read_state(uint32_t tile, double* h, double* hu, double* hv, std::string* err);
+  bool read_state_bits(uint32_t tile, float* planes, std::string* err);
+  bool read_ctl(uint32_t tile, TileCtl& out, std::string* err);
+  bool read_partials(uint32_t tile, Partial* out, std::string* err);
+  bool prime(std::string* err);
+  bool length_pass(uint32_t tile, float max_dt, std::string* err);
+  bool wait(std::string* err);
+
+  uint32_t tile_count() const { return uint32_t(host_.size()); }
+  const TileDesc& desc(uint32_t tile) const { return host_[tile]; }
+  uint64_t cells(uint32_t tile) const { return uint64_t(host_[tile].nx) * host_[tile].ny; }
+  uint64_t total_cells() const { return total_cells_; }
+  uint32_t items() const { return n_items_; }
+  int grid() const { return grid_; }
+  BlockShape shape() const { return shape_; }
+  bool fixed_ops() const { return fixed_; }
+  cudaStream_t stream() const { return stream_; }
+  int device() const { return device_; }
+  TileDesc* device_descs() const { return d_desc_; }
+  float* device_state(uint32_t tile, uint32_t copy) const { return host_[tile].state[copy]; }
+  bool any_manning() const;
+
+ private:
+  bool check(cudaError_t e, std::string* err, const char* what);
+  bool layout_items(BlockShape shape, const std::vector<uint32_t>& order, std::string* err);
+  bool ensure_staging(size_t bytes, std::string* err);
+  bool push_desc(uint32_t tile, std::string* err);
+
+  int device_ = -1;
+  bool fixed_ = false;
+  BlockShape shape_ = BlockShape::k32x32;
+  cudaStream_t stream_ = nullptr;
+  char* base_ = nullptr;  // the one allocation
+  size_t bytes_ = 0;
+  std::vector<TileDesc> host_;  // the descriptors as the device holds them
+  TileDesc* d_desc_ = nullptr;
+  TileCtl* d_ctl_ = nullptr;
+  WorkCtl* d_work_ = nullptr;
+  uint32_t* d_item_tile_ = nullptr;  // the tile of each work item (null for one tile)
+  uint32_t n_items_ = 0;
+  int grid_ = 0;
+  uint64_t total_cells_ = 0;
+  void* staging_ = nullptr;  // device staging for uploads and read-backs
+  size_t staging_bytes_ = 0;
+  std::vector<uint32_t> order_;
+};
+
+// Waits for a stream with a time limit (WLCUDA_WAIT_S seconds, default 300): a wait that passes it
+// returns cudaErrorTimeout-like failure through `timed_out` instead of blocking forever.
+cudaError_t wait_stream(cudaStream_t s, bool* timed_out);
+
+uint64_t fnv1a_floats(const float* v, size_t n, uint64_t hash = 0xcbf29ce484222325ull);
+
+}  // namespace wlc

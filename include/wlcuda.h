@@ -1,0 +1,178 @@
+/* wlcuda — the live-water tick on a GB300 (sm_103a), behind a C ABI.
+ *
+ * A drop-in for the reference's GPU step, engine::water_live::DeviceStep
+ * (systems/water_live/include/systems/water_live/water_live.h:158-256) and its hash
+ * (water_live.h:259). The scheme is the reference's: the hydrostatic reconstruction over the
+ * central-upwind flux on h, hu, hv in FP32, every operation in the reference's order with no
+ * contraction, so a step's bytes equal the reference CPU restatement's bit for bit.
+ *
+ * Conventions (water_live.h:152-157, water_live.cpp:83-86):
+ *  - Every call that moves data between host and device waits for the device; wl_enqueue_steps is
+ *    the asynchronous `record` analogue and may be captured into a CUDA graph.
+ *  - int-returning calls give WL_OK or a WL_ERR_* code and, when `err` is non-null, a message
+ *    (truncated to err_len). uint64-returning calls give 0 on an error.
+ *  - A misfit size is refused with nothing changed. A null or destroyed handle refuses everything
+ *    (water_live_tests.cpp:38-47).
+ *  - Input arrays are read and never kept; the step owns every device buffer.
+ *  - One host thread per handle; no internal locking.
+ */
+#ifndef WLCUDA_H
+#define WLCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t, without the CUDA headers. Null is the legacy default stream. */
+typedef struct CUstream_st* wl_stream;
+
+enum {
+  WL_OK = 0,
+  WL_ERR_INVALID = 1,   /* no device / a handle that was never created */
+  WL_ERR_SIZE = 2,      /* an array that does not fit the grid */
+  WL_ERR_CUDA = 3,      /* a CUDA call failed */
+  WL_ERR_ALLOC = 4,     /* device or host memory could not be had */
+  WL_ERR_REFUSED = 5,   /* a call the step's state refuses (advance with a coarser source clock) */
+  WL_ERR_UNFINISHED = 6,/* advance ran its most batches without landing */
+  WL_ERR_TIMEOUT = 7,   /* a wait for the device passed its limit */
+  WL_ERR_ARGUMENT = 8   /* an argument out of its range */
+};
+
+/* engine::water_state::Config (domain/water_state/include/domain/water_state/water_state.h:83-99),
+ * the fields the step reads: carried, water_density and rows_per_job are not read
+ * (water_live.h:164-166). `device` stands in for the reference's gfx::Device. */
+typedef struct wl_config {
+  uint32_t nx;
+  uint32_t ny;
+  double cell_m;
+  double gravity;
+  double cfl;
+  double dry_depth_m;
+  uint8_t west_open;  /* water_state::Edge: 0 closed (a wall), 1 open */
+  uint8_t east_open;
+  uint8_t south_open;
+  uint8_t north_open;
+  int32_t device;
+} wl_config;
+
+/* water_live::Ops (water_live.h:62) and StepOptions (water_live.h:105-110). */
+enum { WL_OPS_NATIVE = 0, WL_OPS_FIXED = 1 };
+typedef struct wl_options {
+  uint8_t ops;
+  uint8_t stored_faces;
+} wl_options;
+
+/* water_live::StepParams (water_live.h:66-88), mirrored with its 120-byte layout and the offsets
+ * the reference pins (water_live_tests.cpp:22-36). The CUDA kernels take their own argument
+ * structs; this one documents and checks the contract. */
+typedef struct wl_step_params {
+  uint64_t state_in, state_out, bed, manning, source, partials, ledger;
+  uint32_t nx, ny, groups_x, group_count, flags;
+  float cell_m, gravity, cfl, dry_depth_m, max_dt, source_scale;
+  uint32_t pad;
+  uint64_t faces_x, faces_y;
+} wl_step_params;
+
+/* water_live.h:90-97 */
+#define WL_FLAG_WEST_OPEN 1u
+#define WL_FLAG_EAST_OPEN 2u
+#define WL_FLAG_SOUTH_OPEN 4u
+#define WL_FLAG_NORTH_OPEN 8u
+#define WL_FLAG_MANNING 16u
+#define WL_FLAG_SOURCE 32u
+#define WL_FLAG_COMPENSATE 64u
+#define WL_FLAG_STORED_FACES 128u
+#define WL_STATE_PLANES 4u /* water_live.h:102: h, hu, hv, the source's remainder */
+#define WL_GROUP_SIDE 16u  /* water_live.h:140 */
+
+/* water_live::WaterPartial (water_live.h:114-121), 32 bytes: one record per 16 x 16 group. */
+typedef struct wl_partial {
+  float speed_x, speed_y, source_m3, open_m3, roundoff_m3, pad[3];
+} wl_partial;
+
+/* water_live::WaterLedger (water_live.h:124-137), 48 bytes, as the device holds it. */
+typedef struct wl_ledger_bits {
+  float time_hi, time_lo, source_hi, source_lo, open_hi, open_lo, roundoff_hi, roundoff_lo;
+  float remaining_s, dt;
+  uint32_t steps, pad;
+} wl_ledger_bits;
+
+/* water_live::Ledger (water_live.h:143-150). */
+typedef struct wl_ledger {
+  double source_m3, open_edge_out_m3, roundoff_m3, time_s, remaining_s;
+  uint64_t steps;
+} wl_ledger;
+
+typedef struct wl_step wl_step;
+
+/* ---- the plain step: water_live::DeviceStep (water_live.cpp:105-639) ---------------------- */
+
+/* DeviceStep::create (water_live.cpp:105-210): the state dry over a bed of zero, the ledger empty. */
+int wl_create(const wl_config* config, const wl_options* options, wl_step** out, char* err,
+              size_t err_len);
+/* DeviceStep::destroy (water_live.cpp:212-229). Null is a no-op. */
+void wl_destroy(wl_step* step);
+/* DeviceStep::valid (water_live.h:170). */
+int wl_valid(const wl_step* step);
+/* DeviceStep::cell_count / group_count (water_live.h:174-175); 0 for an invalid handle. */
+uint32_t wl_cell_count(const wl_step* step);
+uint32_t wl_group_count(const wl_step* step);
+
+/* DeviceStep::write_state (water_live.cpp:271-314): each array n = nx * ny doubles, rounded to
+ * float; plane 3 zeroed; the ledger emptied; the source clock restarted. */
+int wl_write_state(wl_step* step, const double* depth, const double* momentum_x,
+                   const double* momentum_y, size_t n, char* err, size_t err_len);
+/* DeviceStep::read_state (water_live.cpp:334-347): widened to double. */
+int wl_read_state(wl_step* step, double* depth, double* momentum_x, double* momentum_y, size_t n,
+                  char* err, size_t err_len);
+/* DeviceStep::read_state_bits (water_live.cpp:316-332): count = 4 * nx * ny floats, by plane. */
+int wl_read_state_bits(wl_step* step, float* planes, size_t count, char* err, size_t err_len);
+/* DeviceStep::read_ledger (water_live.cpp:349-381): a flush, then the pairs widened. */
+int wl_read_ledger(wl_step* step, wl_ledger* out, char* err, size_t err_len);
+
+/* DeviceStep::set_bed (water_live.cpp:439-447): bed_m - datum_m in double, rounded once. */
+int wl_set_bed(wl_step* step, const double* bed_m, size_t n, double datum_m, char* err,
+               size_t err_len);
+/* DeviceStep::set_manning (water_live.cpp:449-463): n = 0 turns friction off. */
+int wl_set_manning(wl_step* step, const double* manning, size_t n, char* err, size_t err_len);
+/* DeviceStep::set_source (water_live.cpp:465-486): n = 0 turns sources off; `every` > 1 applies
+ * the source on one step in `every`, `every` times over; `compensate` keeps plane 3. */
+int wl_set_source(wl_step* step, const double* source_m_per_s, size_t n, uint32_t every,
+                  int compensate, char* err, size_t err_len);
+
+/* DeviceStep::record (water_live.cpp:488-568) onto a stream: `count` ticks of
+ * min(stable step, max_dt, time left), one kernel launch each; nothing waits. Every per-tick
+ * quantity (which copy holds the state, the step's length, the ledger, the source clock) lives on
+ * the device, so a captured graph of these launches may be replayed any number of times. */
+int wl_enqueue_steps(wl_step* step, wl_stream stream, uint32_t count, float max_dt);
+/* DeviceStep::run_steps (water_live.cpp:570-574): enqueued on the step's own stream and waited for. */
+int wl_run_steps(wl_step* step, uint32_t count, float max_dt, char* err, size_t err_len);
+/* DeviceStep::advance (water_live.cpp:594-632): the steps taken, 0 on an error or a refusal. */
+uint64_t wl_advance(wl_step* step, double duration_s, char* err, size_t err_len);
+/* DeviceStep::state_hash (water_live.cpp:634-639): FNV-1a over all four planes' floats. */
+uint64_t wl_state_hash(wl_step* step, char* err, size_t err_len);
+
+/* Diagnosis (water_live.h:214-224; water_live.cpp:383-437). */
+int wl_read_partials_bits(wl_step* step, wl_partial* out, size_t count, char* err, size_t err_len);
+int wl_read_ledger_bits(wl_step* step, wl_ledger_bits* out, char* err, size_t err_len);
+int wl_run_length_pass(wl_step* step, float max_dt, char* err, size_t err_len);
+
+/* water_live::hash_floats (water_live.cpp:90-101). */
+uint64_t wl_hash_floats(const float* values, size_t count);
+
+/* The step's own stream (a cudaStream_t), for callers that order work against it. */
+wl_stream wl_step_stream(wl_step* step);
+
+/* The device-resident state in place, for callers that keep their data on the device (no host
+ * copy): the current copy's four planes (4 * nx * ny floats, plane by plane) and the bed. Valid
+ * until the next call on the handle. */
+int wl_device_planes(wl_step* step, float** planes, float** bed, char* err, size_t err_len);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* WLCUDA_H */
