@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Benchmark of the live-water tick on a GB300 (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload plain_2048|plain_256|tiles_4096]
+
+The metric is water cell-updates per second. A bench step is one pass of the workload over its
+configuration: for the default (plain_2048, the throughput configuration) 500 ticks of one
+2048 x 2048 tile from the same seeded initial state. `value` runs with the inputs resident in HBM
+(each step restores the initial state from a device copy, untimed work between steps flushes L2);
+`e2e` runs the same steps through the C ABI with host buffers: upload of the state, bed and source,
+the ticks, and the read-back of the state, every step.
+
+`--impl reference` times the reference's CPU tick (the FP64 solver, water_state::Solver::step,
+restated in oracle/ and checked byte for byte against the reference's own build) on this host's
+cores, on the same workload, a bounded number of ticks a step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_FLUSH_BYTES = 512 << 20  # larger than the GB300's L2 (129 MB)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (every 200 ms)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.file:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names[1:], parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------
+# the reference's CPU tick (the oracle's FP64 restatement of water_state::Solver::step)
+
+def cpu_baseline(tile, threads: int, budget_s: float = 12.0):
+    """Times the reference CPU tick on `tile` with `threads` host threads; bounded sample."""
+    import oracle  # the CPU baseline leg: the oracle's restatement of the reference CPU tick
+    g = oracle.Grid(tile.nx, tile.ny, tile.cell_m)
+    s = oracle.Solver64(g, threads)
+    s.set_state(tile.h, tile.hu, tile.hv)
+    s.set_inputs(tile.bed, None, tile.source)
+    max_dt = tile.meta.get("max_dt", 0.01)
+    t0 = time.perf_counter()
+    s.step(max_dt)
+    one = time.perf_counter() - t0
+    ticks = max(1, min(200, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(ticks):
+        s.step(max_dt)
+    dt = time.perf_counter() - t0
+    return {"value": tile.cells * ticks / dt, "unit": "cell-updates/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{ticks} ticks of the {tile.nx}x{tile.ny} tile (after 1 untimed), FP64 "
+                      f"reference CPU tick restated in oracle/, {threads} threads"}
+
+
+def run_reference(args, tile, rank, world):
+    """--impl reference: the reference CPU tick on this host's cores, on rank 0 only."""
+    if rank != 0:
+        return None
+    import oracle
+    threads = os.cpu_count() or 1
+    g = oracle.Grid(tile.nx, tile.ny, tile.cell_m)
+    s = oracle.Solver64(g, threads)
+    s.set_state(tile.h, tile.hu, tile.hv)
+    s.set_inputs(tile.bed, None, tile.source)
+    max_dt = tile.meta.get("max_dt", 0.01)
+    ticks_per_step = 2
+    for _ in range(args.warmup):
+        for _ in range(ticks_per_step):
+            s.step(max_dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _ in range(ticks_per_step):
+            s.step(max_dt)
+    dt = time.perf_counter() - t0
+    value = tile.cells * ticks_per_step * args.steps / dt
+    sample = (f"{ticks_per_step} ticks a step of the {tile.nx}x{tile.ny} tile, FP64 reference "
+              f"CPU tick (oracle/ restatement, byte-equal to the reference's build), {threads} "
+              "threads")
+    return {
+        "impl": "reference", "metric": "water cell-updates/s", "value": value,
+        "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fBm terrain)",
+        "config": {"workload": tile.meta.get("name"), "cells": tile.cells,
+                   "ticks_per_step": ticks_per_step},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+# ---------------------------------------------------------------------------------------------
+# our arm
+
+def run_plain(args, tile, rank, world):
+    import torch
+    from game_engine_gb300 import lib, water_live as wl
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    L = lib()
+    step = wl.DeviceStep()
+    cfg = wl.Config(tile.nx, tile.ny, tile.cell_m, device=dev)
+    assert step.create(cfg), step.error
+    ticks = tile.meta["ticks"]
+    max_dt = tile.meta["max_dt"]
+    n = tile.cells
+    assert step.set_bed(tile.bed, 0.0), step.error
+    if tile.source is not None:
+        assert step.set_source(tile.source), step.error
+    assert step.write_state(tile.h, tile.hu, tile.hv), step.error
+    # The initial state as float planes on the device, restored before every step.
+    init = torch.from_numpy(step.read_state_bits()).to(f"cuda:{dev}")
+    s_ptr = step.stream()
+    stream = torch.cuda.ExternalStream(s_ptr)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def one_step():
+        rc = L.wl_write_state_device(step.handle, C.c_void_p(init.data_ptr()), s_ptr)
+        assert rc == 0, rc
+        assert step.record(s_ptr, ticks, max_dt), step.error
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+
+    for _ in range(args.warmup):
+        one_step()
+        flush_l2()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with Clocks(dev) as clocks:
+        for k in range(args.steps):
+            starts[k].record(stream)
+            one_step()
+            ends[k].record(stream)
+            flush_l2()
+        torch.cuda.synchronize(dev)
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = args.steps * (ticks + 2)
+
+    # The dominant kernel's average launch, from the same events: every launch of a step but two
+    # (the restore and the prime, a few microseconds) is a tick, enqueued ahead of the device, so
+    # a step's time over its ticks is the tick's duration with the gap between launches included.
+    tick_ms = ms / args.steps / ticks
+    bytes_per_cell = 28.0 + (4.0 if tile.source is not None else 0.0) + 32.0 / 256.0
+    algo_bytes = bytes_per_cell * n
+    achieved = algo_bytes / (tick_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "tick_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                tr = json.load(f)
+            traffic = tr.get(tile.meta.get("name"))
+        except Exception:
+            traffic = None
+    ledger = step.read_ledger()
+
+    # e2e: the public C ABI with host buffers (pinned), every step uploads and reads back.
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).pin_memory()
+    h_h, h_hu, h_hv, h_bed = pin(tile.h), pin(tile.hu), pin(tile.hv), pin(tile.bed)
+    h_src = pin(tile.source) if tile.source is not None else None
+    o_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    o_hu = torch.empty(n, dtype=torch.float64).pin_memory()
+    o_hv = torch.empty(n, dtype=torch.float64).pin_memory()
+    dp = C.POINTER(C.c_double)
+    ptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), dp)
+    err = C.create_string_buffer(256)
+
+    def e2e_step():
+        assert L.wl_set_bed(step.handle, ptr(h_bed), n, 0.0, err, 256) == 0, err.value
+        if h_src is not None:
+            assert L.wl_set_source(step.handle, ptr(h_src), n, 1, 0, err, 256) == 0, err.value
+        assert L.wl_write_state(step.handle, ptr(h_h), ptr(h_hu), ptr(h_hv), n, err, 256) == 0
+        assert L.wl_run_steps(step.handle, ticks, max_dt, err, 256) == 0, err.value
+        assert L.wl_read_state(step.handle, ptr(o_h), ptr(o_hu), ptr(o_hv), n, err, 256) == 0
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush_l2()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_s += time.perf_counter() - t0
+    h2d = n * 8 * (4 + (1 if h_src is not None else 0))
+    d2h = n * 8 * 3
+
+    total_cells = n * ticks * args.steps * world
+    value = total_cells / (ms * 1e-3)
+    e2e_value = total_cells / e2e_s
+    out = {
+        "metric": "water cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded 6-octave fBm terrain 0-50 m, depth U[0,0.5] m, rain 1e-5 m/tick",
+        "config": {"workload": f"plain tick {tile.nx}x{tile.ny}, {ticks} ticks from the same "
+                               "initial state, closed edges, max_dt 0.01 s",
+                   "cells": n, "ticks_per_step": ticks, "max_dt": max_dt,
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (8 planes of 16.8 MB = 134 MB per tick) and an "
+                         "L2 flush (512 MB write) between steps, outside the timed events",
+                   "cfl_limited_ticks": None,
+                   "ledger_steps_last_run": ledger["steps"] if ledger else None},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": algo_bytes,
+                     "bytes_per_cell": bytes_per_cell, "avg_launch_ms": tick_ms,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain_2048")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from game_engine_gb300 import workloads
+
+    if args.workload == "plain_2048":
+        tile = workloads.plain_2048()
+    elif args.workload == "plain_256":
+        tile = workloads.plain_256()
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+
+    if args.impl == "reference":
+        out = run_reference(args, tile, rank, world)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("WL_BENCH_NCCL") else "gloo")
+    out = run_plain(args, tile, rank, world)
+    if rank == 0:
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(tile, os.cpu_count() or 1)
+        else:
+            out["cpu_baseline"] = None
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,6 +1,6 @@
 """wlcuda: the reference engine's live-water tick on a GB300 (sm_103a), behind a C ABI.
 
-``libwlcuda.so`` (built by :mod:`game_engine_gb300.build`) holds the CUDA kernels and the C ABI
+``libwlcuda.so`` (built by :mod:`game_engine_gb300.buildlib`) holds the CUDA kernels and the C ABI
 declared in ``include/wlcuda.h``. :mod:`game_engine_gb300.water_live` mirrors the reference's
 ``water_live::DeviceStep`` over that ABI; :mod:`game_engine_gb300.batch` the batched tiles and
 :mod:`game_engine_gb300.adjoint` the checkpointed reverse tick.
@@ -28,7 +28,7 @@ def lib() -> C.CDLL:
     if _lib is None:
         if not os.path.exists(LIB_PATH):
             raise LibraryMissing(
-                f"{LIB_PATH} is missing: build it with `python -m game_engine_gb300.build` "
+                f"{LIB_PATH} is missing: build it with `python -m game_engine_gb300.buildlib` "
                 "(nvcc, sm_103a); there is no CPU fallback")
         from . import _abi
         _lib = _abi.bind(C.CDLL(LIB_PATH))
@@ -36,5 +36,5 @@ def lib() -> C.CDLL:
 
 
 def build(verbose: bool = False) -> str:
-    from .build import build as _build
+    from .buildlib import build as _build
     return _build(verbose=verbose)

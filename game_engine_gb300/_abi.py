@@ -78,6 +78,7 @@ SIGNATURES = {
     "wl_run_length_pass": (C.c_int, [C.c_void_p, C.c_float, *_err]),
     "wl_hash_floats": (C.c_uint64, [_fp, C.c_size_t]),
     "wl_step_stream": (wl_stream, [C.c_void_p]),
+    "wl_write_state_device": (C.c_int, [C.c_void_p, C.c_void_p, wl_stream]),
     "wl_device_planes": (C.c_int, [C.c_void_p, C.POINTER(_fp), C.POINTER(_fp), *_err]),
 }
 

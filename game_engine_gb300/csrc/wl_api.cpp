@@ -334,6 +334,16 @@ wl_stream wl_step_stream(wl_step* s) {
   return valid(s) ? reinterpret_cast<wl_stream>(s->set.stream()) : nullptr;
 }
 
+int wl_write_state_device(wl_step* s, const float* planes, wl_stream stream) {
+  if (!valid(s)) return WL_ERR_INVALID;
+  if (planes == nullptr) return WL_ERR_ARGUMENT;
+  if (cudaSetDevice(s->set.device()) != cudaSuccess) return WL_ERR_CUDA;
+  cudaStream_t st = stream == nullptr ? s->set.stream() : reinterpret_cast<cudaStream_t>(stream);
+  if (wlc::launch_write_state_f32(s->set.device_descs(), 0, s->cells, planes, st) != cudaSuccess)
+    return WL_ERR_CUDA;
+  return s->set.enqueue_prime(st) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
+}
+
 int wl_device_planes(wl_step* s, float** planes, float** bed, char* err, size_t err_len) {
   if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
   wlc::TileCtl c;

@@ -607,6 +607,26 @@ __global__ void write_state_kernel(TileDesc* tiles, uint32_t tile, const double*
   }
 }
 
+// write_state from float planes already on the device (planes 0-2 copied, plane 3 zeroed).
+__global__ void write_state_f32_kernel(TileDesc* tiles, uint32_t tile, const float* src) {
+  const TileDesc& T = tiles[tile];
+  const size_t n = size_t(T.nx) * T.ny;
+  float* p = T.state[T.ctl->cur];
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x) {
+    p[i] = src[i];
+    p[n + i] = src[n + i];
+    p[2 * n + i] = src[2 * n + i];
+    p[3 * n + i] = 0.0f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    LedgerBits empty = {};
+    empty.remaining_s = __int_as_float(0x7f800000);
+    T.ctl->ledger = empty;
+    T.ctl->src_phase = 0u;
+  }
+}
+
 // set_bed / set_manning / set_source's conversion: (x - datum) in double, rounded once.
 __global__ void plane_kernel(float* dst, const double* src, size_t n, double datum) {
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
@@ -741,6 +761,12 @@ static int grid_for(size_t n) {
 cudaError_t launch_write_state(TileDesc* tiles, uint32_t tile, size_t n, const double* h,
                                const double* hu, const double* hv, cudaStream_t s) {
   write_state_kernel<<<grid_for(n), 256, 0, s>>>(tiles, tile, h, hu, hv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_write_state_f32(TileDesc* tiles, uint32_t tile, size_t n, const float* planes,
+                                   cudaStream_t s) {
+  write_state_f32_kernel<<<grid_for(n), 256, 0, s>>>(tiles, tile, planes);
   return cudaGetLastError();
 }
 

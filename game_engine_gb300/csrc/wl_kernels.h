@@ -38,6 +38,8 @@ cudaError_t launch_length_pass(bool fixed, const TileDesc* tiles, uint32_t tile,
                                cudaStream_t s);
 cudaError_t launch_write_state(TileDesc* tiles, uint32_t tile, size_t n, const double* h,
                                const double* hu, const double* hv, cudaStream_t s);
+cudaError_t launch_write_state_f32(TileDesc* tiles, uint32_t tile, size_t n, const float* planes,
+                                   cudaStream_t s);
 cudaError_t launch_plane(float* dst, const double* src, size_t n, double datum, cudaStream_t s);
 cudaError_t launch_read_state(const TileDesc* tiles, uint32_t tile, size_t n, double* h,
                               double* hu, double* hv, cudaStream_t s);

@@ -1,0 +1,146 @@
+"""Seeded synthetic inputs for the benchmark configurations (no dataset exists for this path).
+
+Terrain is fBm: six octaves of value noise on an integer-hash lattice (the reference's `mix`,
+water_live_device_tests.cpp:50-56, so the lattice is the same on every host), lacunarity 2, gain
+0.5, base period side / 4, smoothstep-weighted bilinear interpolation in double, normalised to
+[0, H]. Every configuration has a fixed 64-bit seed.
+
+  plain_256   256 x 256, H 20 m, dry but for a centred 32 x 32 column of 2 m; 1000 ticks.
+  plain_2048  2048 x 2048, H 50 m, depth U[0, 0.5] m, rain 1e-5 m a tick; 500 ticks.
+  tiles_4096  4096 tiles, sides from {64, 96, 128, 192, 256, 384, 512}, each its own fBm (H 20 m)
+              and a 2 m column of 32 x 32 at a seeded place; 200 ticks.
+  adjoint_512 512 x 512 and tiles_256_adjoint: see game_engine_gb300.adjoint.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEEDS = {
+    "plain_256": 0x5EED_0001_C0FF_EE01,
+    "plain_2048": 0x5EED_0002_C0FF_EE02,
+    "tiles_4096": 0x5EED_0003_C0FF_EE03,
+    "adjoint_512": 0x5EED_0004_C0FF_EE04,
+    "tiles_256_adjoint": 0x5EED_0005_C0FF_EE05,
+}
+MAX_DT = 0.01  # the reference's rule dt = min(stable, max_dt) with a fixed max_dt
+MASK = 0xFFFFFFFF
+
+
+def mix(x, y):
+    x = np.asarray(x, dtype=np.uint64)
+    y = np.asarray(y, dtype=np.uint64)
+    h = ((x * 0x9E3779B1) & MASK) ^ ((((y + 0x7F4A7C15) & MASK) * 0x85EBCA77) & MASK)
+    h ^= h >> 15
+    h = (h * 0x2C1B3C6D) & MASK
+    h ^= h >> 12
+    return h
+
+
+def _lattice(ix, iy, salt):
+    return mix(ix + (salt & MASK), iy ^ ((salt >> 32) & MASK)).astype(np.float64) / 4294967296.0
+
+
+def fbm(nx: int, ny: int, height: float, seed: int, octaves: int = 6) -> np.ndarray:
+    """nx * ny heights in [0, height] (row-major, cell (x, y) at y * nx + x)."""
+    side = max(nx, ny)
+    base = max(side / 4.0, 1.0)
+    ys, xs = np.meshgrid(np.arange(ny, dtype=np.float64), np.arange(nx, dtype=np.float64),
+                         indexing="ij")
+    total = np.zeros((ny, nx))
+    amp = 1.0
+    period = base
+    for o in range(octaves):
+        salt = (seed * (o + 1) * 0x9E3779B97F4A7C15 + o) & 0xFFFFFFFFFFFFFFFF
+        fx = xs / period
+        fy = ys / period
+        ix = np.floor(fx)
+        iy = np.floor(fy)
+        tx = fx - ix
+        ty = fy - iy
+        sx = tx * tx * (3.0 - 2.0 * tx)
+        sy = ty * ty * (3.0 - 2.0 * ty)
+        ix = ix.astype(np.uint64)
+        iy = iy.astype(np.uint64)
+        v00 = _lattice(ix, iy, salt)
+        v10 = _lattice(ix + 1, iy, salt)
+        v01 = _lattice(ix, iy + 1, salt)
+        v11 = _lattice(ix + 1, iy + 1, salt)
+        a = v00 + (v10 - v00) * sx
+        b = v01 + (v11 - v01) * sx
+        total += amp * (a + (b - a) * sy)
+        amp *= 0.5
+        period = max(period / 2.0, 1.0)
+    lo, hi = total.min(), total.max()
+    span = hi - lo if hi > lo else 1.0
+    return ((total - lo) / span * height).ravel()
+
+
+@dataclass
+class Tile:
+    """One rectangle's inputs, as the API takes them (doubles, nx * ny each)."""
+    nx: int
+    ny: int
+    bed: np.ndarray
+    h: np.ndarray
+    hu: np.ndarray = None
+    hv: np.ndarray = None
+    source: np.ndarray | None = None
+    cell_m: float = 1.0
+    meta: dict = field(default_factory=dict)
+
+    def __post_init__(self):
+        n = self.nx * self.ny
+        if self.hu is None:
+            self.hu = np.zeros(n)
+        if self.hv is None:
+            self.hv = np.zeros(n)
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny
+
+
+def column(nx, ny, x0, y0, side=32, depth=2.0):
+    h = np.zeros((ny, nx))
+    h[y0:y0 + side, x0:x0 + side] = depth
+    return h.ravel()
+
+
+def plain_256() -> Tile:
+    n = 256
+    bed = fbm(n, n, 20.0, SEEDS["plain_256"])
+    h = column(n, n, n // 2 - 16, n // 2 - 16)
+    return Tile(n, n, bed, h, meta=dict(ticks=1000, max_dt=MAX_DT, name="plain_256"))
+
+
+def plain_2048(side: int = 2048) -> Tile:
+    bed = fbm(side, side, 50.0, SEEDS["plain_2048"])
+    rng = np.random.Generator(np.random.PCG64(SEEDS["plain_2048"] & 0xFFFFFFFF))
+    h = rng.uniform(0.0, 0.5, side * side)
+    rain = np.full(side * side, 1e-5 / MAX_DT)  # 1e-5 m a tick at dt = max_dt
+    return Tile(side, side, bed, h, source=rain,
+                meta=dict(ticks=500, max_dt=MAX_DT, name=f"plain_{side}"))
+
+
+TILE_SIDES = (64, 96, 128, 192, 256, 384, 512)
+
+
+def tile_sides(count: int, seed: int, sides=TILE_SIDES):
+    rng = np.random.Generator(np.random.PCG64(seed & 0xFFFFFFFF))
+    return [int(sides[k]) for k in rng.integers(0, len(sides), count)]
+
+
+def tiles_4096(count: int = 4096, sides=None, seed: int | None = None, with_bed: bool = True):
+    """The batched workload: `count` tiles of seeded sides, each its own fBm and 2 m column."""
+    seed = SEEDS["tiles_4096"] if seed is None else seed
+    sides = tile_sides(count, seed) if sides is None else sides
+    rng = np.random.Generator(np.random.PCG64((seed >> 32) & 0xFFFFFFFF))
+    out = []
+    for k, s in enumerate(sides):
+        bed = fbm(s, s, 20.0, seed + 7919 * (k + 1)) if with_bed else np.zeros(s * s)
+        x0 = int(rng.integers(0, s - 32 + 1))
+        y0 = int(rng.integers(0, s - 32 + 1))
+        out.append(Tile(s, s, bed, column(s, s, x0, y0), meta=dict(index=k)))
+    return out

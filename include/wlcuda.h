@@ -166,6 +166,12 @@ uint64_t wl_hash_floats(const float* values, size_t count);
 /* The step's own stream (a cudaStream_t), for callers that order work against it. */
 wl_stream wl_step_stream(wl_step* step);
 
+/* write_state from device memory: `planes` holds 4 * nx * ny floats on the step's device (plane 3
+ * is ignored and zeroed, as write_state does); the ledger is emptied, the source clock restarted and
+ * the records primed, all enqueued on `stream` (null: the step's own) without waiting. For callers
+ * whose inputs already live on the device. */
+int wl_write_state_device(wl_step* step, const float* planes, wl_stream stream);
+
 /* The device-resident state in place, for callers that keep their data on the device (no host
  * copy): the current copy's four planes (4 * nx * ny floats, plane by plane) and the bed. Valid
  * until the next call on the handle. */
