@@ -1,10 +1,11 @@
 // The C ABI of include/wlcuda.h: water_live::DeviceStep's calls over a TileSet of one tile.
 // Each function names the reference call it stands in for (systems/water_live/src/water_live.cpp).
-#include "../../include/wlcuda.h"
+#include "wlcuda.h"
 
 #include "wl_tiles.h"
 
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -107,9 +108,14 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
   if (config->north_open) s->flags |= WL_FLAG_NORTH_OPEN;
   if (s->options.stored_faces) s->flags |= WL_FLAG_STORED_FACES;
   t.open_edges = s->flags & 15u;
+  // The block shape: 32 x 32 unless WLCUDA_BLOCK_ROWS names 16 or 64 (a tuning override).
+  wlc::BlockShape shape = wlc::BlockShape::k32x32;
+  if (const char* rows = std::getenv("WLCUDA_BLOCK_ROWS")) {
+    if (std::strcmp(rows, "16") == 0) shape = wlc::BlockShape::k32x16;
+    if (std::strcmp(rows, "64") == 0) shape = wlc::BlockShape::k32x64;
+  }
   std::string msg;
-  if (!s->set.create(config->device, {t}, s->options.ops == WL_OPS_FIXED,
-                     wlc::BlockShape::k32x32, {}, &msg)) {
+  if (!s->set.create(config->device, {t}, s->options.ops == WL_OPS_FIXED, shape, {}, &msg)) {
     delete s;
     return cuda_fail(err, err_len, msg);
   }

@@ -4,18 +4,23 @@
 // tile). It replaces the reference's two passes a step, the length pass `dt_main`
 // (water_step.slang:412-479) and the update `update_main` (slang:555-757), with one:
 //
-//   - Work items are blocks of BX x BY cells of some tile; CTAs take them in order from a counter.
-//   - Each item chooses the step's length itself, from the tile's control block: the largest
+//   - A work item is a band of one tile: 32 columns by H rows. Each warp takes items from a
+//     counter and steps them alone; no item waits for another and no barrier spans warps.
+//   - The item chooses the step's length itself from the tile's control block: the largest
 //     speeds of the last update (kept by atomicMax on their bits, exact in any order), the time
 //     left and max_dt, the same arithmetic as dt_main's thread 0.
-//   - The item that takes a tile's first block also folds the last update's records into the
-//     ledger, in dt_main's own order (256 lanes over the records, then a fixed tree), so the
+//   - The warp that takes a tile's first item also folds the last update's records into the
+//     ledger in dt_main's own order (256 lanes over the records, then a fixed tree), so the
 //     ledger's bits are the reference's.
-//   - A block stages its cells and a one-cell halo in shared memory ({h, z, u, v}, the edges' ghost
-//     cells built as the reference builds them), computes each of its faces once into shared
-//     memory (both cells of a face take the same value, which is what the reference's gather
-//     computes twice), updates its cells, writes the three planes once, and writes one record per
-//     16 x 16 group with the reference's 256-slot tree.
+//   - The warp marches down its band, a lane a column. Each row it loads the row two ahead (the
+//     loads are in flight while it computes), computes the north face of its cell and its west
+//     face (the west neighbour's state by shuffle), takes its east face from the lane to its
+//     right by shuffle, and updates the cell; the north face is carried up as the next row's south
+//     face. Each face is computed once, so both cells of a face take the same value, which is
+//     what the reference's gather computes twice. The band's side columns (the west neighbour of
+//     lane 0 and the east face of the last lane) are computed first, a row a lane.
+//   - Every 16 rows the warp writes the records of the two 16 x 16 groups it covers, with the
+//     reference's 256-slot tree over each group's volumes.
 //   - The last item of a tile to finish commits the tick: the new ledger, the flipped copy and
 //     record buffer, the new largest speeds and the source's clock.
 //
@@ -24,77 +29,102 @@
 #include "wl_device.cuh"
 #include "wl_kernels.h"
 
-#include <cstdio>
-
 namespace wlc {
 
 namespace {
 
-template <int BX, int BY>
-struct Shape {
-  static constexpr int kCellsX = BX + 2;
-  static constexpr int kCells = (BX + 2) * (BY + 2);
-  static constexpr int kFacesX = (BX + 1) * BY;
-  static constexpr int kFacesY = BX * (BY + 1);
-  static constexpr int kGroupsX = BX / 16;
-  static constexpr int kGroupsY = BY / 16;
-  static constexpr int kGroups = kGroupsX * kGroupsY;
-  static constexpr int kRowStep = kThreads / BX;     // rows between a thread's cells
-  static constexpr int kPerThread = BX * BY / kThreads;
-  static constexpr size_t kSmem = sizeof(float4) * (kCells + kFacesX + kFacesY) +
-                                  sizeof(float) * 3 * BX * BY;
-  static_assert(BX % 32 == 0 && BY % 16 == 0, "blocks are whole warps wide and whole groups tall");
-  static_assert(BX * BY >= kThreads && (BX * BY) % kThreads == 0, "whole cells per thread");
+constexpr int kStrip = 32;        // an item is a warp wide
+constexpr int kWarpsPerCta = 4;   // 128 threads a CTA
+constexpr int kCtaThreads = 32 * kWarpsPerCta;
+
+// A warp's shared memory: the band's side columns and a ring of 16 rows of per-cell volumes.
+template <int H>
+struct WarpMem {
+  static constexpr size_t kBytes = 2 * H * sizeof(float4) + 3 * 16 * kStrip * sizeof(float);
+  float4* west;  // H: {h, z, u, v} of the column west of lane 0, row by row
+  float4* east;  // H: the east face of the band's last live lane, row by row
+  float* ring;   // 3 x 16 x 32: the source, open-edge and roundoff volumes of the last 16 rows
 };
 
-struct ItemInfo {
-  uint32_t tile, bx, by, cur, rec, fold, apply_source;
-  float dt, scale;
-};
+template <int H>
+__device__ __forceinline__ WarpMem<H> warp_mem(int warp) {
+  extern __shared__ float4 smem[];
+  char* base = reinterpret_cast<char*>(smem) + size_t(warp) * WarpMem<H>::kBytes;
+  WarpMem<H> m;
+  m.west = reinterpret_cast<float4*>(base);
+  m.east = m.west + H;
+  m.ring = reinterpret_cast<float*>(m.east + H);
+  return m;
+}
 
-// dt_main's sums (slang:417-456): lane t adds records t, t + 256, ... in order, then the fixed
-// 256-slot tree. Leaves the three sums in s[0], s[256], s[512]. When `zero`, the records' sums are
-// cleared after they are read (a flush or a length pass; slang:432-435). When `maxima`, also
-// returns the records' largest speeds in s_ab (the length pass reads them from the records).
-__device__ void fold_sums(Partial* rec, uint32_t groups, bool zero, float* s, uint32_t* s_ab,
-                          bool maxima) {
+__device__ __forceinline__ uint32_t item_tile_of(const uint32_t* item_tile, uint32_t item) {
+  return item_tile == nullptr ? 0u : item_tile[item];
+}
+
+// ---- the ledger ---------------------------------------------------------------------------
+
+// dt_main's sums (slang:417-456) by one warp: virtual lane L of 256 adds records L, L + 256, ...
+// in order, then the fixed 256-slot tree. Leaves the three sums in s[0], s[256], s[512].
+__device__ void fold_warp(const Partial* rec, uint32_t groups, float* s) {
+  const int lane = threadIdx.x & 31;
+  for (int vl = lane; vl < int(kGroupCells); vl += 32) {
+    float src = 0.0f, opn = 0.0f, rnd = 0.0f;
+    for (uint32_t gi = vl; gi < groups; gi += kGroupCells) {
+      const Partial p = rec[gi];
+      src = __fadd_rn(src, p.source_m3);
+      opn = __fadd_rn(opn, p.open_m3);
+      rnd = __fadd_rn(rnd, p.roundoff_m3);
+    }
+    s[vl] = src;
+    s[kGroupCells + vl] = opn;
+    s[2 * kGroupCells + vl] = rnd;
+  }
+  __syncwarp();
+  for (int stride = kGroupCells / 2; stride > 0; stride >>= 1) {
+    for (int vl = lane; vl < stride; vl += 32) {
+      s[vl] = __fadd_rn(s[vl], s[vl + stride]);
+      s[kGroupCells + vl] = __fadd_rn(s[kGroupCells + vl], s[kGroupCells + vl + stride]);
+      s[2 * kGroupCells + vl] =
+          __fadd_rn(s[2 * kGroupCells + vl], s[2 * kGroupCells + vl + stride]);
+    }
+    __syncwarp();
+  }
+}
+
+// The same with a CTA of 256 threads, the records' sums cleared after they are read and their
+// largest speeds returned (the length pass, slang:412-456).
+__device__ void fold_cta(Partial* rec, uint32_t groups, float* s, uint32_t* s_ab) {
   const int t = threadIdx.x;
+  if (t == 0) {
+    s_ab[0] = 0u;
+    s_ab[1] = 0u;
+  }
+  __syncthreads();
   float src = 0.0f, opn = 0.0f, rnd = 0.0f;
   uint32_t a = 0u, b = 0u;
-  for (uint32_t gi = t; gi < groups; gi += kThreads) {
+  for (uint32_t gi = t; gi < groups; gi += kGroupCells) {
     const Partial p = rec[gi];
     src = __fadd_rn(src, p.source_m3);
     opn = __fadd_rn(opn, p.open_m3);
     rnd = __fadd_rn(rnd, p.roundoff_m3);
     a = max(a, __float_as_uint(p.speed_x));
     b = max(b, __float_as_uint(p.speed_y));
-    if (zero) {
-      rec[gi].source_m3 = 0.0f;
-      rec[gi].open_m3 = 0.0f;
-      rec[gi].roundoff_m3 = 0.0f;
-    }
+    rec[gi].source_m3 = 0.0f;
+    rec[gi].open_m3 = 0.0f;
+    rec[gi].roundoff_m3 = 0.0f;
   }
   s[t] = src;
-  s[kThreads + t] = opn;
-  s[2 * kThreads + t] = rnd;
+  s[kGroupCells + t] = opn;
+  s[2 * kGroupCells + t] = rnd;
+  atomicMax(&s_ab[0], a);
+  atomicMax(&s_ab[1], b);
   __syncthreads();
-#pragma unroll
-  for (int stride = kThreads / 2; stride > 0; stride >>= 1) {
+  for (int stride = kGroupCells / 2; stride > 0; stride >>= 1) {
     if (t < stride) {
       s[t] = __fadd_rn(s[t], s[t + stride]);
-      s[kThreads + t] = __fadd_rn(s[kThreads + t], s[kThreads + t + stride]);
-      s[2 * kThreads + t] = __fadd_rn(s[2 * kThreads + t], s[2 * kThreads + t + stride]);
+      s[kGroupCells + t] = __fadd_rn(s[kGroupCells + t], s[kGroupCells + t + stride]);
+      s[2 * kGroupCells + t] = __fadd_rn(s[2 * kGroupCells + t], s[2 * kGroupCells + t + stride]);
     }
-    __syncthreads();
-  }
-  if (maxima) {
-    if (t == 0) {
-      s_ab[0] = 0u;
-      s_ab[1] = 0u;
-    }
-    __syncthreads();
-    atomicMax(&s_ab[0], a);
-    atomicMax(&s_ab[1], b);
     __syncthreads();
   }
 }
@@ -117,15 +147,16 @@ __device__ void ledger_update(LedgerBits& l, float src, float opn, float rnd, fl
   }
 }
 
-__device__ __forceinline__ void copy_ledger(volatile LedgerBits* dst, const volatile LedgerBits* src) {
+__device__ __forceinline__ void copy_ledger(volatile LedgerBits* dst,
+                                            const volatile LedgerBits* src) {
   const volatile uint32_t* s = reinterpret_cast<const volatile uint32_t*>(src);
   volatile uint32_t* d = reinterpret_cast<volatile uint32_t*>(dst);
 #pragma unroll
   for (int i = 0; i < 12; ++i) d[i] = s[i];
 }
 
-// The end of a work item (thread 0, after the block's writes were fenced): the block's largest
-// speeds into the tile's running maxima, and, for the tile's last item, the commit.
+// The end of a work item (one thread, after the item's writes were fenced): its largest speeds
+// into the tile's running maxima and, for the tile's last item, the commit.
 __device__ void finish_item(const TileDesc& T, uint32_t amax, uint32_t bmax, bool tick) {
   TileCtl* ctl = T.ctl;
   atomicMax(&ctl->max_a, amax);
@@ -151,172 +182,234 @@ __device__ void finish_item(const TileDesc& T, uint32_t amax, uint32_t bmax, boo
   __threadfence();
 }
 
-// The records of one block from per-cell values in shared memory: the largest speeds (exact in any
-// order) reduced by shuffles, and each of the three sums by the reference's 256-slot tree
-// (slang:338-371) where any of its cells holds a non-zero value.
-template <int BX, int BY>
-__device__ void write_records(const TileDesc& T, Partial* rec_out, uint32_t bx, uint32_t by,
-                              const float* s_sum, uint32_t* s_gmax, float* s_gsum,
-                              const uint32_t (&amax)[BY / 16], const uint32_t (&bmax)[BY / 16],
-                              bool need_src, bool need_opn, bool need_rnd, uint32_t& blk_a,
-                              uint32_t& blk_b) {
-  using S = Shape<BX, BY>;
-  const int t = threadIdx.x;
-  const int lane = t & 31, warp = t >> 5;
-  const int c = t % BX;
-  const int gc = c / 16;
-  // Speeds: the 16 lanes of a half-warp hold one group's column range.
+// ---- the records ----------------------------------------------------------------------------
+
+// One group's 256-slot tree (slang:346-358) by one warp: lane l holds slots l + 32 k (slot
+// i = ly * 16 + lx), so strides 128, 64 and 32 are adds in registers and 16..1 are shuffles.
+// `ring` holds the 16 rows x 32 lanes of one quantity; the group is columns 16 gc .. 16 gc + 15.
+__device__ __forceinline__ float group_tree(const float* ring, int gc) {
+  const int lane = threadIdx.x & 31;
+  float v[8];
 #pragma unroll
-  for (int gr = 0; gr < S::kGroupsY; ++gr) {
-    uint32_t a = amax[gr], b = bmax[gr];
+  for (int k = 0; k < 8; ++k) {
+    const int slot = lane + 32 * k;
+    v[k] = ring[(slot >> 4) * kStrip + 16 * gc + (slot & 15)];
+  }
+  const float a0 = __fadd_rn(v[0], v[4]), a1 = __fadd_rn(v[1], v[5]);
+  const float a2 = __fadd_rn(v[2], v[6]), a3 = __fadd_rn(v[3], v[7]);
+  const float b0 = __fadd_rn(a0, a2), b1 = __fadd_rn(a1, a3);
+  float c = __fadd_rn(b0, b1);
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) {
-      a = max(a, __shfl_xor_sync(0xffffffffu, a, o));
-      b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
-    }
-    if ((lane & 15) == 0) {
-      atomicMax(&s_gmax[2 * (gr * S::kGroupsX + gc)], a);
-      atomicMax(&s_gmax[2 * (gr * S::kGroupsX + gc) + 1], b);
-    }
+  for (int stride = 16; stride > 0; stride >>= 1) {
+    const float o = __shfl_down_sync(0xffffffffu, c, stride);
+    if (lane < stride) c = __fadd_rn(c, o);
   }
-  // Sums: one warp per (group, quantity) tree. Lane l holds slots l + 32 k, k = 0..7; slot
-  // i = ly * 16 + lx of the group.
-  const bool need[3] = {need_src, need_opn, need_rnd};
-  for (int job = warp; job < 3 * S::kGroups; job += kThreads / 32) {
-    const int q = job / S::kGroups, grp = job % S::kGroups;
-    float res = 0.0f;
-    if (need[q]) {
-      const int gr = grp / S::kGroupsX, gcc = grp % S::kGroupsX;
-      const float* base = s_sum + q * BX * BY + (gr * 16) * BX + gcc * 16;
-      float v[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int slot = lane + 32 * k;
-        v[k] = base[(slot >> 4) * BX + (slot & 15)];
-      }
-      // strides 128, 64, 32: slot + 128 is k + 4, + 64 is k + 2, + 32 is k + 1
-      const float a0 = __fadd_rn(v[0], v[4]), a1 = __fadd_rn(v[1], v[5]);
-      const float a2 = __fadd_rn(v[2], v[6]), a3 = __fadd_rn(v[3], v[7]);
-      const float b0 = __fadd_rn(a0, a2), b1 = __fadd_rn(a1, a3);
-      float cc = __fadd_rn(b0, b1);
-#pragma unroll
-      for (int stride = 16; stride > 0; stride >>= 1) {
-        const float o = __shfl_down_sync(0xffffffffu, cc, stride);
-        if (lane < stride) cc = __fadd_rn(cc, o);
-      }
-      res = cc;
-    }
-    if (lane == 0) s_gsum[grp * 3 + q] = res;
-  }
-  __syncthreads();
-  if (t < S::kGroups) {
-    const int gr = t / S::kGroupsX, gcc = t % S::kGroupsX;
-    const uint32_t gxg = bx * S::kGroupsX + gcc, gyg = by * S::kGroupsY + gr;
-    if (gxg < T.groups_x && gyg < T.groups_y) {
-      float4* dst = reinterpret_cast<float4*>(rec_out + size_t(gyg) * T.groups_x + gxg);
-      dst[0] = make_float4(__uint_as_float(s_gmax[2 * t]), __uint_as_float(s_gmax[2 * t + 1]),
-                           s_gsum[t * 3 + 0], s_gsum[t * 3 + 1]);
-      dst[1] = make_float4(s_gsum[t * 3 + 2], 0.0f, 0.0f, 0.0f);
-    }
-  }
-  if (t == 0) {
-    uint32_t a = 0u, b = 0u;
-    for (int g = 0; g < S::kGroups; ++g) {
-      a = max(a, s_gmax[2 * g]);
-      b = max(b, s_gmax[2 * g + 1]);
-    }
-    blk_a = a;
-    blk_b = b;
-  }
+  return c;
 }
 
-__device__ __forceinline__ uint32_t item_tile_of(const uint32_t* item_tile, uint32_t item) {
-  return item_tile == nullptr ? 0u : item_tile[item];
+// The records of the two groups a warp covers in one group row (slang:338-371). `ga`/`gb` are
+// each lane's largest speeds over the group row; the ring holds the volumes of its 16 rows (rows
+// past the grid's edge zero). need_* names the quantities some cell holds. Returns the two groups'
+// largest speeds (lane 0 holds them).
+__device__ __forceinline__ void group_records(const TileDesc& T, Partial* rec_out, int X0,
+                                              int group_row, uint32_t ga, uint32_t gb,
+                                              const float* ring, bool need_src, bool need_opn,
+                                              bool need_rnd, uint32_t& ia, uint32_t& ib) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) {
+    ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
+    gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
+  }
+  const uint32_t a1 = __shfl_sync(0xffffffffu, ga, 16), b1 = __shfl_sync(0xffffffffu, gb, 16);
+  float s0 = 0.0f, s1 = 0.0f, o0 = 0.0f, o1 = 0.0f, r0 = 0.0f, r1 = 0.0f;
+  if (need_src) {
+    s0 = group_tree(ring, 0);
+    s1 = group_tree(ring, 1);
+  }
+  if (need_opn) {
+    o0 = group_tree(ring + 16 * kStrip, 0);
+    o1 = group_tree(ring + 16 * kStrip, 1);
+  }
+  if (need_rnd) {
+    r0 = group_tree(ring + 32 * kStrip, 0);
+    r1 = group_tree(ring + 32 * kStrip, 1);
+  }
+  if (lane == 0) {
+    const uint32_t gyg = uint32_t(group_row);
+    const uint32_t gx0 = uint32_t(X0 / 16);
+    if (gyg < T.groups_y) {
+      if (gx0 < T.groups_x) {
+        float4* d = reinterpret_cast<float4*>(rec_out + size_t(gyg) * T.groups_x + gx0);
+        d[0] = make_float4(__uint_as_float(ga), __uint_as_float(gb), s0, o0);
+        d[1] = make_float4(r0, 0.0f, 0.0f, 0.0f);
+      }
+      if (gx0 + 1u < T.groups_x) {
+        float4* d = reinterpret_cast<float4*>(rec_out + size_t(gyg) * T.groups_x + gx0 + 1u);
+        d[0] = make_float4(__uint_as_float(a1), __uint_as_float(b1), s1, o1);
+        d[1] = make_float4(r1, 0.0f, 0.0f, 0.0f);
+      }
+    }
+    ia = max(ia, max(ga, a1));
+    ib = max(ib, max(gb, b1));
+  }
+  __syncwarp();
 }
 
-// One block of one tile, one tick.
-template <bool FIXED, bool MANNING, int BX, int BY>
-__device__ void step_block(const TileDesc& T, const ItemInfo& it, float max_dt, float4* s_cell,
-                           float4* s_fx, float4* s_fy, float* s_sum, uint32_t* s_gmax,
-                           float* s_gsum, uint32_t& blk_a, uint32_t& blk_b) {
-  using S = Shape<BX, BY>;
+// ---- the march ------------------------------------------------------------------------------
+
+struct Item {
+  uint32_t cur, rec, apply_source;
+  float dt, scale;
+  int X0, Y0;
+};
+
+// {h, z, u, v} of a cell from its loaded h, hu, hv and bed (slang:303-314).
+template <bool FIXED>
+__device__ __forceinline__ float4 velocities(float h, float hu, float hv, float z, float dry) {
+  const bool wet = h >= dry;
+  const float u = wet ? Ops<FIXED>::div(hu, h) : 0.0f;
+  const float v = wet ? Ops<FIXED>::div(hv, h) : 0.0f;
+  return make_float4(h, z, u, v);
+}
+
+template <bool FIXED>
+__device__ __forceinline__ float4 load_cell(const float* ph, const float* phu, const float* phv,
+                                            const float* bed, int i, float dry) {
+  return velocities<FIXED>(ph[i], phu[i], phv[i], bed[i], dry);
+}
+
+// An x face between cells L and R; a y face between cells S and N (slang:274-292, 597-628).
+template <bool FIXED>
+__device__ __forceinline__ float4 face_x(float g, float hg, const float4& L, const float4& R) {
+  return face<FIXED>(g, hg, L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w);
+}
+template <bool FIXED>
+__device__ __forceinline__ float4 face_y(float g, float hg, const float4& S, const float4& N) {
+  return face<FIXED>(g, hg, S.x, S.y, S.w, S.z, N.x, N.y, N.w, N.z);
+}
+
+__device__ __forceinline__ float4 shfl_up4(const float4& v) {
+  return make_float4(__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1),
+                     __shfl_up_sync(0xffffffffu, v.z, 1), __shfl_up_sync(0xffffffffu, v.w, 1));
+}
+__device__ __forceinline__ float4 shfl_down4(const float4& v) {
+  return make_float4(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1),
+                     __shfl_down_sync(0xffffffffu, v.z, 1), __shfl_down_sync(0xffffffffu, v.w, 1));
+}
+
+// One item: a band of 32 columns by up to H rows of one tile, one tick.
+template <bool FIXED, bool MANNING, int H>
+__device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, uint32_t& ia,
+                      uint32_t& ib) {
   using O = Ops<FIXED>;
-  const int t = threadIdx.x;
-  const uint32_t nx = T.nx, ny = T.ny;
-  const size_t n = size_t(nx) * ny;
-  const int X0 = int(it.bx) * BX, Y0 = int(it.by) * BY;
+  const int lane = threadIdx.x & 31;
+  const int nx = int(T.nx), ny = int(T.ny);
+  const size_t n = size_t(T.nx) * T.ny;
+  const int X0 = it.X0, Y0 = it.Y0;
+  const int gx = X0 + lane;
+  const bool col = gx < nx;
+  const int last = min(kStrip - 1, nx - 1 - X0);  // the band's last live lane
+  const int rows = min(H, ny - Y0);
   const float* in = T.state[it.cur];
   float* out = T.state[it.cur ^ 1u];
-  const float g = T.gravity, dry = T.dry, half_g = __fmul_rn(0.5f, g);
+  const float* ph = in;
+  const float* phu = in + n;
+  const float* phv = in + 2 * n;
+  float* qh = out;
+  float* qhu = out + n;
+  float* qhv = out + 2 * n;
+  const float* bed = T.bed;
+  const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
   const float dt = it.dt;
   const uint32_t flags = T.flags;
-  const bool stepping = dt > 0.0f;
+  Partial* rec_out = T.rec[it.rec ^ 1u];
+  uint32_t ga = 0u, gb = 0u;
 
-  if (t < 2 * S::kGroups) s_gmax[t] = 0u;
-
-  if (stepping) {
-    // Stage the block and its halo: {h, z, u, v}, ghosts at the edges (slang:597-628).
-    const float sw = (flags & kFlagWestOpen) ? 1.0f : -1.0f;
-    const float se = (flags & kFlagEastOpen) ? 1.0f : -1.0f;
-    const float ss = (flags & kFlagSouthOpen) ? 1.0f : -1.0f;
-    const float sn = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
-    for (int p = t; p < S::kCells; p += kThreads) {
-      const int py = p / S::kCellsX, px = p - py * S::kCellsX;
-      const int gx = X0 + px - 1, gy = Y0 + py - 1;
-      const bool inx = gx >= 0 && gx < int(nx), iny = gy >= 0 && gy < int(ny);
-      int sx = gx, sy = gy;
-      int ghost = 0;  // 1: the normal is u, 2: the normal is v
-      float sign = 1.0f;
-      bool use = inx && iny;
-      if (!use && iny) {
-        if (gx == -1) { sx = 0; sign = sw; ghost = 1; use = true; }
-        else if (gx == int(nx)) { sx = int(nx) - 1; sign = se; ghost = 1; use = true; }
-      } else if (!use && inx) {
-        if (gy == -1) { sy = 0; sign = ss; ghost = 2; use = true; }
-        else if (gy == int(ny)) { sy = int(ny) - 1; sign = sn; ghost = 2; use = true; }
+  if (!(dt > 0.0f)) {
+    // A step of no length: the state as it is, to the bit (slang:576-585).
+    for (int j = 0; j < rows; ++j) {
+      const int gy = Y0 + j;
+      if (col) {
+        const int i = gy * nx + gx;
+        const float h0 = ph[i], hu0 = phu[i], hv0 = phv[i];
+        qh[i] = h0;
+        qhu[i] = hu0;
+        qhv[i] = hv0;
+        out[3 * n + i] = in[3 * n + i];
+        float ax, ay;
+        cell_speeds<FIXED>(g, dry, h0, hu0, hv0, ax, ay);
+        ga = max(ga, __float_as_uint(ax));
+        gb = max(gb, __float_as_uint(ay));
       }
-      float4 cv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (use) {
-        const size_t i = size_t(sy) * nx + sx;
-        const float h = in[i];
-        const bool wet = h >= dry;
-        float u = wet ? O::div(in[n + i], h) : 0.0f;
-        float v = wet ? O::div(in[2 * n + i], h) : 0.0f;
-        if (ghost == 1) u = __fmul_rn(sign, u);
-        if (ghost == 2) v = __fmul_rn(sign, v);
-        cv = make_float4(h, T.bed[i], u, v);
-      }
-      s_cell[p] = cv;
-    }
-    __syncthreads();
-    // Every face of the block once: x faces west of each column, y faces south of each row.
-    for (int f = t; f < S::kFacesX + S::kFacesY; f += kThreads) {
-      float4 res = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (f < S::kFacesX) {
-        const int r = f / (BX + 1), c = f - r * (BX + 1);
-        if (Y0 + r < int(ny) && X0 + c - 1 < int(nx)) {
-          const float4 L = s_cell[(r + 1) * S::kCellsX + c];
-          const float4 R = s_cell[(r + 1) * S::kCellsX + c + 1];
-          res = face<FIXED>(g, half_g, L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w);
-        }
-        s_fx[f] = res;
-      } else {
-        const int f2 = f - S::kFacesX;
-        const int r = f2 / BX, c = f2 - r * BX;
-        if (X0 + c < int(nx) && Y0 + r - 1 < int(ny)) {
-          const float4 Sc = s_cell[r * S::kCellsX + c + 1];
-          const float4 Nc = s_cell[(r + 1) * S::kCellsX + c + 1];
-          res = face<FIXED>(g, half_g, Sc.x, Sc.y, Sc.w, Sc.z, Nc.x, Nc.y, Nc.w, Nc.z);
-        }
-        s_fy[f2] = res;
+      if ((j & 15) == 15 || j == rows - 1) {
+        group_records(T, rec_out, X0, gy / 16, ga, gb, wm.ring, false, false, false, ia, ib);
+        ga = gb = 0u;
       }
     }
-    __syncthreads();
-  } else {
-    __syncthreads();
+    return;
   }
 
-  // The update of each cell (slang:630-753).
+  const float sw = (flags & kFlagWestOpen) ? 1.0f : -1.0f;
+  const float se = (flags & kFlagEastOpen) ? 1.0f : -1.0f;
+  const float ss = (flags & kFlagSouthOpen) ? 1.0f : -1.0f;
+  const float sn = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
+
+  // The band's side columns, a row a lane: the west neighbour of lane 0 as {h, z, u, v} (a ghost
+  // at the west edge, slang:597-600), and the east face of the last live lane (against its east
+  // neighbour, or its ghost at the east edge, slang:605-608).
+  for (int j0 = 0; j0 < rows; j0 += 32) {
+    const int j = j0 + lane;
+    if (j < rows) {
+      const int row = (Y0 + j) * nx;
+      float4 w;
+      if (X0 > 0) {
+        w = load_cell<FIXED>(ph, phu, phv, bed, row + X0 - 1, dry);
+      } else {
+        w = load_cell<FIXED>(ph, phu, phv, bed, row, dry);
+        w.z = __fmul_rn(sw, w.z);
+      }
+      const float4 cl = load_cell<FIXED>(ph, phu, phv, bed, row + X0 + last, dry);
+      float4 e;
+      if (X0 + last + 1 < nx) {
+        e = load_cell<FIXED>(ph, phu, phv, bed, row + X0 + last + 1, dry);
+      } else {
+        e = cl;
+        e.z = __fmul_rn(se, cl.z);
+      }
+      wm.west[j] = w;
+      wm.east[j] = face_x<FIXED>(g, hg, cl, e);
+    }
+  }
+  __syncwarp();
+
+  // The first row, its south face, and the row above it in flight.
+  const int gxc = col ? gx : 0;  // dead lanes read a live column and write nothing
+  int i = Y0 * nx + gxc;
+  float hu = phu[i], hv = phv[i];
+  float src = it.apply_source ? T.source[i] : 0.0f;
+  float4 c = velocities<FIXED>(ph[i], hu, hv, bed[i], dry);
+  float4 fs;
+  {
+    float4 s;
+    if (Y0 > 0) {
+      s = load_cell<FIXED>(ph, phu, phv, bed, i - nx, dry);
+    } else {
+      s = c;
+      s.w = __fmul_rn(ss, c.w);
+    }
+    fs = face_y<FIXED>(g, hg, s, c);
+  }
+  float nh = 0.0f, nhu = 0.0f, nhv = 0.0f, nz = 0.0f, nsrc = 0.0f;
+  if (Y0 + 1 < ny) {
+    const int k = i + nx;
+    nh = ph[k];
+    nhu = phu[k];
+    nhv = phv[k];
+    nz = bed[k];
+    if (it.apply_source) nsrc = T.source[k];
+  }
+
   const float cell_m = T.cell_m;
   const float area = __fmul_rn(cell_m, cell_m);
   const float lam = O::div(dt, cell_m);
@@ -324,194 +417,190 @@ __device__ void step_block(const TileDesc& T, const ItemInfo& it, float max_dt, 
   const bool src_on = it.apply_source != 0u;
   const bool comp = (flags & kFlagCompensate) != 0u;
   const bool manning = MANNING && (flags & kFlagManning) != 0u;
+  const bool any_open_band = (flags & 15u) != 0u;
   const float scale = it.scale;
-  const int c = t % BX, r0 = t / BX;
-  const int gx = X0 + c;
-  uint32_t amax[BY / 16], bmax[BY / 16];
-#pragma unroll
-  for (int k = 0; k < BY / 16; ++k) amax[k] = bmax[k] = 0u;
-  bool any_rnd = false;
-#pragma unroll
-  for (int k = 0; k < S::kPerThread; ++k) {
-    const int r = r0 + k * S::kRowStep;
-    const int gy = Y0 + r;
-    float ax = 0.0f, ay = 0.0f, csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
-    if (gx < int(nx) && gy < int(ny)) {
-      const size_t i = size_t(gy) * nx + gx;
-      if (!stepping) {
-        // A step of no length: the state as it is, to the bit (slang:576-585).
-        const float h0 = in[i], hu0 = in[n + i], hv0 = in[2 * n + i];
-        out[i] = h0;
-        out[n + i] = hu0;
-        out[2 * n + i] = hv0;
-        out[3 * n + i] = in[3 * n + i];
-        cell_speeds<FIXED>(g, dry, h0, hu0, hv0, ax, ay);
-      } else {
-        const float4 fw = s_fx[r * (BX + 1) + c];
-        const float4 fe = s_fx[r * (BX + 1) + c + 1];
-        const float4 fs = s_fy[r * BX + c];
-        const float4 fn = s_fy[(r + 1) * BX + c];
-        const float h0 = s_cell[(r + 1) * S::kCellsX + c + 1].x;
-        if ((flags & 15u) != 0u) {
-          if (gx == 0 && (flags & kFlagWestOpen)) copn = __fsub_rn(copn, __fmul_rn(fw.x, edge_volume));
-          if (gx + 1 == int(nx) && (flags & kFlagEastOpen)) copn = __fadd_rn(copn, __fmul_rn(fe.x, edge_volume));
-          if (gy == 0 && (flags & kFlagSouthOpen)) copn = __fsub_rn(copn, __fmul_rn(fs.x, edge_volume));
-          if (gy + 1 == int(ny) && (flags & kFlagNorthOpen)) copn = __fadd_rn(copn, __fmul_rn(fn.x, edge_volume));
-        }
-        // U' = U - dt/dx ((F_e - F_w) + (F_n - F_s)) (slang:653-668)
-        float h = __fsub_rn(h0, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.x, fw.x), __fsub_rn(fn.x, fs.x))));
-        float hu = __fsub_rn(in[n + i], __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.y, fw.z), __fsub_rn(fn.w, fs.w))));
-        float hv = __fsub_rn(in[2 * n + i], __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.w, fw.w), __fsub_rn(fn.y, fs.z))));
-        if (h < 0.0f) {
-          crnd = __fsub_rn(crnd, __fmul_rn(h, area));
-          h = 0.0f;
-          any_rnd = true;
-        }
-        float residual = 0.0f;
-        if (comp) residual = in[3 * n + i];
-        if (src_on && comp) {
-          const float owed = __fmul_rn(T.source[i], dt);
-          const float scaled = __fmul_rn(owed, scale);
-          const float target = __fadd_rn(scaled, residual);
-          float h2 = h;
-          if (target >= 0.0f) {
-            h2 = __fadd_rn(h, target);
-          } else {
-            const float want = -target;
-            const float taken = want < h ? want : h;
-            h2 = __fsub_rn(h, taken);
-          }
-          const float applied = __fsub_rn(h2, h);
-          const float left = __fsub_rn(target, applied);
-          residual = (h2 == 0.0f && target < 0.0f) ? 0.0f : left;
-          csrc = __fadd_rn(csrc, __fmul_rn(applied, area));
-          h = h2;
-        } else if (src_on) {
-          const float owed = __fmul_rn(T.source[i], dt);
-          const float added = __fmul_rn(owed, scale);
-          if (added >= 0.0f) {
-            h = __fadd_rn(h, added);
-            csrc = __fadd_rn(csrc, __fmul_rn(added, area));
-          } else {
-            const float want = -added;
-            const float taken = want < h ? want : h;
-            h = __fsub_rn(h, taken);
-            csrc = __fsub_rn(csrc, __fmul_rn(taken, area));
-          }
-        }
-        if (h >= dry) {
-          if (manning) {
-            // (hu)' = (hu)* / (1 + dt g n^2 |u*| / h^(4/3)) (slang:722-744)
-            const float nn = T.manning[i];
-            const float u = O::div(hu, h);
-            const float v = O::div(hv, h);
-            const float sp = O::sqrt(__fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)));
-            const float cb = O::cbrt(h);
-            const float k3 = __fmul_rn(__fmul_rn(__fmul_rn(g, nn), nn), sp);
-            const float k = O::div(k3, __fmul_rn(h, cb));
-            const float denom = __fadd_rn(1.0f, __fmul_rn(dt, k));
-            hu = O::div(hu, denom);
-            hv = O::div(hv, denom);
-          }
-        } else {
-          hu = 0.0f;
-          hv = 0.0f;
-        }
-        out[i] = h;
-        out[n + i] = hu;
-        out[2 * n + i] = hv;
-        if (comp) out[3 * n + i] = residual;
-        cell_speeds<FIXED>(g, dry, h, hu, hv, ax, ay);
-      }
-    }
-    const int ci = r * BX + c;
-    s_sum[ci] = csrc;
-    s_sum[BX * BY + ci] = copn;
-    s_sum[2 * BX * BY + ci] = crnd;
-    const int gr = (k * S::kRowStep) / 16;  // r0 < kRowStep <= 16: a compile-time group row
-    amax[gr] = max(amax[gr], __float_as_uint(ax));
-    bmax[gr] = max(bmax[gr], __float_as_uint(ay));
-  }
-  const bool need_rnd = __syncthreads_or(any_rnd) != 0;
-  const bool touches_open =
-      ((flags & kFlagWestOpen) && X0 == 0) || ((flags & kFlagEastOpen) && X0 + BX >= int(nx)) ||
-      ((flags & kFlagSouthOpen) && Y0 == 0) || ((flags & kFlagNorthOpen) && Y0 + BY >= int(ny));
-  write_records<BX, BY>(T, T.rec[it.rec ^ 1u], it.bx, it.by, s_sum, s_gmax, s_gsum, amax, bmax,
-                        stepping && src_on, stepping && touches_open, need_rnd, blk_a, blk_b);
-}
+  bool opn_seen = false, rnd_seen = false;
 
-template <int BX, int BY>
-__device__ __forceinline__ void carve(float4*& s_cell, float4*& s_fx, float4*& s_fy,
-                                      float*& s_sum) {
-  using S = Shape<BX, BY>;
-  extern __shared__ float4 smem[];
-  s_cell = smem;
-  s_fx = s_cell + S::kCells;
-  s_fy = s_fx + S::kFacesX;
-  s_sum = reinterpret_cast<float*>(s_fy + S::kFacesY);
+  for (int j = 0; j < rows; ++j) {
+    const int gy = Y0 + j;
+    // The north cell: the row loaded last iteration, or the north ghost (slang:621-624).
+    float4 nc;
+    const float hu_n = nhu, hv_n = nhv, src_n = nsrc;
+    if (gy + 1 < ny) {
+      nc = velocities<FIXED>(nh, nhu, nhv, nz, dry);
+    } else {
+      nc = c;
+      nc.w = __fmul_rn(sn, c.w);
+    }
+    // The row two ahead, in flight while this row computes.
+    if (gy + 2 < ny) {
+      const int k = i + 2 * nx;
+      nh = ph[k];
+      nhu = phu[k];
+      nhv = phv[k];
+      nz = bed[k];
+      if (src_on) nsrc = T.source[k];
+    }
+    const float4 fn = face_y<FIXED>(g, hg, c, nc);
+    float4 w = shfl_up4(c);
+    if (lane == 0) w = wm.west[j];
+    const float4 fw = face_x<FIXED>(g, hg, w, c);
+    float4 fe = shfl_down4(fw);
+    if (lane == last) fe = wm.east[j];
+
+    float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
+    float ax = 0.0f, ay = 0.0f;
+    if (col) {
+      if (any_open_band) {
+        if (gx == 0 && (flags & kFlagWestOpen)) copn = __fsub_rn(copn, __fmul_rn(fw.x, edge_volume));
+        if (gx + 1 == nx && (flags & kFlagEastOpen)) copn = __fadd_rn(copn, __fmul_rn(fe.x, edge_volume));
+        if (gy == 0 && (flags & kFlagSouthOpen)) copn = __fsub_rn(copn, __fmul_rn(fs.x, edge_volume));
+        if (gy + 1 == ny && (flags & kFlagNorthOpen)) copn = __fadd_rn(copn, __fmul_rn(fn.x, edge_volume));
+      }
+      // U' = U - dt/dx ((F_e - F_w) + (F_n - F_s)) (slang:653-668)
+      float h = __fsub_rn(c.x, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.x, fw.x), __fsub_rn(fn.x, fs.x))));
+      float mu = __fsub_rn(hu, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.y, fw.z), __fsub_rn(fn.w, fs.w))));
+      float mv = __fsub_rn(hv, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.w, fw.w), __fsub_rn(fn.y, fs.z))));
+      if (h < 0.0f) {
+        crnd = __fsub_rn(crnd, __fmul_rn(h, area));
+        h = 0.0f;
+      }
+      float residual = 0.0f;
+      if (comp) residual = in[3 * n + i];
+      if (src_on && comp) {
+        const float owed = __fmul_rn(src, dt);
+        const float scaled = __fmul_rn(owed, scale);
+        const float target = __fadd_rn(scaled, residual);
+        float h2 = h;
+        if (target >= 0.0f) {
+          h2 = __fadd_rn(h, target);
+        } else {
+          const float want = -target;
+          const float taken = want < h ? want : h;
+          h2 = __fsub_rn(h, taken);
+        }
+        const float applied = __fsub_rn(h2, h);
+        const float left = __fsub_rn(target, applied);
+        residual = (h2 == 0.0f && target < 0.0f) ? 0.0f : left;
+        csrc = __fadd_rn(csrc, __fmul_rn(applied, area));
+        h = h2;
+      } else if (src_on) {
+        const float owed = __fmul_rn(src, dt);
+        const float added = __fmul_rn(owed, scale);
+        if (added >= 0.0f) {
+          h = __fadd_rn(h, added);
+          csrc = __fadd_rn(csrc, __fmul_rn(added, area));
+        } else {
+          const float want = -added;
+          const float taken = want < h ? want : h;
+          h = __fsub_rn(h, taken);
+          csrc = __fsub_rn(csrc, __fmul_rn(taken, area));
+        }
+      }
+      if (h >= dry) {
+        if (manning) {
+          // (hu)' = (hu)* / (1 + dt g n^2 |u*| / h^(4/3)) (slang:722-744)
+          const float nn = T.manning[i];
+          const float u = O::div(mu, h);
+          const float v = O::div(mv, h);
+          const float sp = O::sqrt(__fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)));
+          const float cb = O::cbrt(h);
+          const float k3 = __fmul_rn(__fmul_rn(__fmul_rn(g, nn), nn), sp);
+          const float k = O::div(k3, __fmul_rn(h, cb));
+          const float denom = __fadd_rn(1.0f, __fmul_rn(dt, k));
+          mu = O::div(mu, denom);
+          mv = O::div(mv, denom);
+        }
+      } else {
+        mu = 0.0f;
+        mv = 0.0f;
+      }
+      qh[i] = h;
+      qhu[i] = mu;
+      qhv[i] = mv;
+      if (comp) out[3 * n + i] = residual;
+      cell_speeds<FIXED>(g, dry, h, mu, mv, ax, ay);
+    }
+    ga = max(ga, __float_as_uint(ax));
+    gb = max(gb, __float_as_uint(ay));
+    const int slot = (j & 15) * kStrip + lane;
+    wm.ring[slot] = csrc;
+    wm.ring[16 * kStrip + slot] = copn;
+    wm.ring[32 * kStrip + slot] = crnd;
+    opn_seen |= copn != 0.0f;
+    rnd_seen |= crnd != 0.0f;
+    if ((j & 15) == 15 || j == rows - 1) {
+      // The group row ends: rows past the grid's edge hold nothing, then the records.
+      for (int r = (j & 15) + 1; r < 16; ++r) {
+        wm.ring[r * kStrip + lane] = 0.0f;
+        wm.ring[(16 + r) * kStrip + lane] = 0.0f;
+        wm.ring[(32 + r) * kStrip + lane] = 0.0f;
+      }
+      __syncwarp();
+      const bool need_opn = __any_sync(0xffffffffu, opn_seen);
+      const bool need_rnd = __any_sync(0xffffffffu, rnd_seen);
+      group_records(T, rec_out, X0, gy / 16, ga, gb, wm.ring, src_on, need_opn, need_rnd, ia, ib);
+      ga = gb = 0u;
+      opn_seen = rnd_seen = false;
+    }
+    // Up one row.
+    c = nc;
+    hu = hu_n;
+    hv = hv_n;
+    src = src_n;
+    fs = fn;
+    i += nx;
+  }
 }
 
 // The persistent tick: every work item of every tile, one tick.
-template <bool FIXED, bool MANNING, int BX, int BY>
-__global__ void __launch_bounds__(kThreads) tick_kernel(TickArgs a) {
-  float4 *s_cell, *s_fx, *s_fy;
-  float* s_sum;
-  carve<BX, BY>(s_cell, s_fx, s_fy, s_sum);
-  __shared__ ItemInfo s_it;
-  __shared__ uint32_t s_gmax[2 * Shape<BX, BY>::kGroups];
-  __shared__ float s_gsum[3 * Shape<BX, BY>::kGroups];
-  __shared__ uint32_t s_ab[2];
-  const int t = threadIdx.x;
+template <bool FIXED, bool MANNING, int H>
+__global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const WarpMem<H> wm = warp_mem<H>(warp);
   for (;;) {
-    if (t == 0) {
-      const uint32_t item = atomicAdd(&a.work->next, 1u);
-      s_it.tile = 0xffffffffu;
-      if (item < a.n_items) {
-        const uint32_t tile = item_tile_of(a.item_tile, item);
-        const TileDesc& T = a.tiles[tile];
-        const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
-        const TileCtl* ctl = T.ctl;
-        s_it.tile = tile;
-        s_it.by = local / T.blocks_x;
-        s_it.bx = local - s_it.by * T.blocks_x;
-        s_it.cur = ctl->cur;
-        s_it.rec = ctl->rec;
-        s_it.fold = local == 0u ? 1u : 0u;
-        const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
-        s_it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
-        const bool src = (T.flags & kFlagSource) != 0u;
-        const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
-        s_it.apply_source = on ? 1u : 0u;
-        s_it.scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
-      }
-    }
-    __syncthreads();
-    if (s_it.tile == 0xffffffffu) break;
-    const ItemInfo it = s_it;
-    const TileDesc& T = a.tiles[it.tile];
-    if (it.fold) {
-      // The ledger's fold of the last update's records (dt_main, slang:417-478).
-      fold_sums(T.rec[it.rec], T.groups_x * T.groups_y, false, s_sum, s_ab, false);
-      if (t == 0) {
-        LedgerBits l = T.ctl->ledger;
-        ledger_update<FIXED>(l, s_sum[0], s_sum[kThreads], s_sum[2 * kThreads],
-                             __uint_as_float(T.ctl->prev_a), __uint_as_float(T.ctl->prev_b),
-                             T.cfl, T.cell_m, a.max_dt);
+    uint32_t item = 0u;
+    if (lane == 0) item = atomicAdd(&a.work->next, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= a.n_items) break;
+    const uint32_t tile = item_tile_of(a.item_tile, item);
+    const TileDesc& T = a.tiles[tile];
+    const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
+    const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+    const TileCtl* ctl = T.ctl;
+    Item it;
+    it.cur = ctl->cur;
+    it.rec = ctl->rec;
+    const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
+    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
+    const bool src = (T.flags & kFlagSource) != 0u;
+    const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
+    it.apply_source = on ? 1u : 0u;
+    it.scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
+    it.X0 = int(bx) * kStrip;
+    it.Y0 = int(by) * H;
+    if (local == 0u) {
+      // The ledger's fold of the last update's records (dt_main, slang:417-478), in the warp's
+      // ring before the march needs it.
+      fold_warp(T.rec[it.rec], T.groups_x * T.groups_y, wm.ring);
+      if (lane == 0) {
+        LedgerBits l = ctl->ledger;
+        ledger_update<FIXED>(l, wm.ring[0], wm.ring[kGroupCells], wm.ring[2 * kGroupCells], pa,
+                             pb, T.cfl, T.cell_m, a.max_dt);
         T.ctl->ledger_next = l;
       }
-      __syncthreads();
+      __syncwarp();
     }
-    uint32_t blk_a = 0u, blk_b = 0u;
-    step_block<FIXED, MANNING, BX, BY>(T, it, a.max_dt, s_cell, s_fx, s_fy, s_sum, s_gmax, s_gsum,
-                                      blk_a, blk_b);
+    uint32_t ia = 0u, ib = 0u;
+    march<FIXED, MANNING, H>(T, it, wm, ia, ib);
     __threadfence();
-    __syncthreads();
-    if (t == 0) finish_item(T, blk_a, blk_b, true);
-    __syncthreads();
+    __syncwarp();
+    if (lane == 0) finish_item(T, ia, ib, true);
+    __syncwarp();
   }
-  if (t == 0) {
+  if (lane == 0) {
     __threadfence();
-    if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x) {
+    if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x * kWarpsPerCta) {
       a.work->next = 0u;
       a.work->exited = 0u;
       __threadfence();
@@ -519,71 +608,70 @@ __global__ void __launch_bounds__(kThreads) tick_kernel(TickArgs a) {
   }
 }
 
-// The records of a state written from the host (prime_main, slang:373-386): one CTA a block.
-template <bool FIXED, int BX, int BY>
-__global__ void __launch_bounds__(kThreads) prime_kernel(TickArgs a) {
-  using S = Shape<BX, BY>;
-  const uint32_t item = blockIdx.x;
+// The records of a state written from the host (prime_main, slang:373-386): a warp an item.
+template <bool FIXED, int H>
+__global__ void __launch_bounds__(kCtaThreads) prime_kernel(TickArgs a) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t item = blockIdx.x * kWarpsPerCta + warp;
   if (item >= a.n_items) return;
-  __shared__ uint32_t s_gmax[2 * S::kGroups];
-  __shared__ float s_gsum[3 * S::kGroups];
-  const int t = threadIdx.x;
+  const WarpMem<H> wm = warp_mem<H>(warp);
   const uint32_t tile = item_tile_of(a.item_tile, item);
   const TileDesc& T = a.tiles[tile];
   const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
   const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
-  const uint32_t cur = T.ctl->cur, rec = T.ctl->rec;
-  const float* in = T.state[cur];
+  const float* in = T.state[T.ctl->cur];
   const size_t n = size_t(T.nx) * T.ny;
-  if (t < 2 * S::kGroups) s_gmax[t] = 0u;
-  const int c = t % BX, r0 = t / BX;
-  const int gx = int(bx) * BX + c;
-  uint32_t amax[BY / 16], bmax[BY / 16];
-#pragma unroll
-  for (int k = 0; k < BY / 16; ++k) amax[k] = bmax[k] = 0u;
-#pragma unroll
-  for (int k = 0; k < S::kPerThread; ++k) {
-    const int r = r0 + k * S::kRowStep;
-    const int gy = int(by) * BY + r;
-    float ax = 0.0f, ay = 0.0f;
-    if (gx < int(T.nx) && gy < int(T.ny)) {
-      const size_t i = size_t(gy) * T.nx + gx;
+  const int nx = int(T.nx), ny = int(T.ny);
+  const int X0 = int(bx) * kStrip, Y0 = int(by) * H;
+  const int gx = X0 + lane;
+  const int rows = min(H, ny - Y0);
+  uint32_t ga = 0u, gb = 0u, ia = 0u, ib = 0u;
+  for (int j = 0; j < rows; ++j) {
+    const int gy = Y0 + j;
+    if (gx < nx) {
+      const int i = gy * nx + gx;
+      float ax, ay;
       cell_speeds<FIXED>(T.gravity, T.dry, in[i], in[n + i], in[2 * n + i], ax, ay);
+      ga = max(ga, __float_as_uint(ax));
+      gb = max(gb, __float_as_uint(ay));
     }
-    const int gr = (k * S::kRowStep) / 16;
-    amax[gr] = max(amax[gr], __float_as_uint(ax));
-    bmax[gr] = max(bmax[gr], __float_as_uint(ay));
+    if ((j & 15) == 15 || j == rows - 1) {
+      group_records(T, T.rec[T.ctl->rec], X0, gy / 16, ga, gb, wm.ring, false, false, false, ia,
+                    ib);
+      ga = gb = 0u;
+    }
   }
-  __syncthreads();
-  uint32_t blk_a = 0u, blk_b = 0u;
-  // The prime's records carry no sums (no tree reads the per-cell sums): they go into the buffer
-  // that holds the current records.
-  write_records<BX, BY>(T, T.rec[rec], bx, by, s_gsum, s_gmax, s_gsum, amax, bmax, false, false,
-                        false, blk_a, blk_b);
   __threadfence();
-  __syncthreads();
-  if (t == 0) finish_item(T, blk_a, blk_b, false);
+  __syncwarp();
+  if (lane == 0) finish_item(T, ia, ib, false);
 }
 
 // dt_main alone, on one tile (slang:412-479): a flush (max_dt 0) or the length pass. The records'
 // sums are folded and cleared; the ledger is written in place.
 template <bool FIXED>
-__global__ void __launch_bounds__(kThreads) length_pass_kernel(const TileDesc* tiles, uint32_t tile,
-                                                              float max_dt) {
-  __shared__ float s[3 * kThreads];
+__global__ void __launch_bounds__(256) length_pass_kernel(const TileDesc* tiles, uint32_t tile,
+                                                          float max_dt) {
+  __shared__ float s[3 * kGroupCells];
   __shared__ uint32_t s_ab[2];
   const TileDesc& T = tiles[tile];
   Partial* rec = T.rec[T.ctl->rec];
-  fold_sums(rec, T.groups_x * T.groups_y, true, s, s_ab, true);
+  fold_cta(rec, T.groups_x * T.groups_y, s, s_ab);
   if (threadIdx.x == 0) {
     LedgerBits l = T.ctl->ledger;
-    ledger_update<FIXED>(l, s[0], s[kThreads], s[2 * kThreads], __uint_as_float(s_ab[0]),
+    ledger_update<FIXED>(l, s[0], s[kGroupCells], s[2 * kGroupCells], __uint_as_float(s_ab[0]),
                          __uint_as_float(s_ab[1]), T.cfl, T.cell_m, max_dt);
     T.ctl->ledger = l;
   }
 }
 
 // ---- uploads and read-backs -------------------------------------------------------------------
+
+__device__ __forceinline__ void reset_ledger(TileCtl* ctl) {
+  LedgerBits empty = {};
+  empty.remaining_s = __int_as_float(0x7f800000);
+  ctl->ledger = empty;
+  ctl->src_phase = 0u;
+}
 
 // write_state's conversion (water_live.cpp:276-282): planes 0-2 rounded from double, plane 3 zero,
 // into the copy that holds the state; the ledger emptied and the source's clock restarted.
@@ -599,12 +687,7 @@ __global__ void write_state_kernel(TileDesc* tiles, uint32_t tile, const double*
     p[2 * n + i] = __double2float_rn(hv[i]);
     p[3 * n + i] = 0.0f;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    LedgerBits empty = {};
-    empty.remaining_s = __int_as_float(0x7f800000);
-    T.ctl->ledger = empty;
-    T.ctl->src_phase = 0u;
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) reset_ledger(T.ctl);
 }
 
 // write_state from float planes already on the device (planes 0-2 copied, plane 3 zeroed).
@@ -619,12 +702,7 @@ __global__ void write_state_f32_kernel(TileDesc* tiles, uint32_t tile, const flo
     p[2 * n + i] = src[2 * n + i];
     p[3 * n + i] = 0.0f;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    LedgerBits empty = {};
-    empty.remaining_s = __int_as_float(0x7f800000);
-    T.ctl->ledger = empty;
-    T.ctl->src_phase = 0u;
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) reset_ledger(T.ctl);
 }
 
 // set_bed / set_manning / set_source's conversion: (x - datum) in double, rounded once.
@@ -658,16 +736,39 @@ __global__ void copy_state_kernel(const TileDesc* tiles, uint32_t tile, float* d
     dst[i] = p[i];
 }
 
-// The tick kernels' shared-memory opt-in is set per device by tick_occupancy(), which the host
-// calls when it creates a step, before any launch or capture.
-template <int BX, int BY>
-struct Launch {
-  template <bool FIXED, bool MANNING>
-  static cudaError_t tick(const TickArgs& a, int grid, cudaStream_t s) {
-    tick_kernel<FIXED, MANNING, BX, BY><<<grid, kThreads, Shape<BX, BY>::kSmem, s>>>(a);
-    return cudaGetLastError();
+template <int H>
+const void* tick_fn(bool fixed, bool manning) {
+  if (fixed)
+    return manning ? (const void*)tick_kernel<true, true, H> : (const void*)tick_kernel<true, false, H>;
+  return manning ? (const void*)tick_kernel<false, true, H> : (const void*)tick_kernel<false, false, H>;
+}
+
+template <int H>
+cudaError_t tick_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = kWarpsPerCta * WarpMem<H>::kBytes;
+  if (fixed) {
+    if (manning) tick_kernel<true, true, H><<<grid, kCtaThreads, smem, s>>>(a);
+    else tick_kernel<true, false, H><<<grid, kCtaThreads, smem, s>>>(a);
+  } else {
+    if (manning) tick_kernel<false, true, H><<<grid, kCtaThreads, smem, s>>>(a);
+    else tick_kernel<false, false, H><<<grid, kCtaThreads, smem, s>>>(a);
   }
-};
+  return cudaGetLastError();
+}
+
+template <int H>
+cudaError_t prime_launch(bool fixed, const TickArgs& a, cudaStream_t s) {
+  const size_t smem = kWarpsPerCta * WarpMem<H>::kBytes;
+  const unsigned grid = (a.n_items + kWarpsPerCta - 1) / kWarpsPerCta;
+  if (fixed) prime_kernel<true, H><<<grid, kCtaThreads, smem, s>>>(a);
+  else prime_kernel<false, H><<<grid, kCtaThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+int grid_for(size_t n) {
+  const size_t b = (n + 255) / 256;
+  return int(b < 4096 ? (b == 0 ? 1 : b) : 4096);
+}
 
 }  // namespace
 
@@ -675,40 +776,37 @@ struct Launch {
 
 size_t tick_smem_bytes(BlockShape shape) {
   switch (shape) {
-    case BlockShape::k32x16: return Shape<32, 16>::kSmem;
-    case BlockShape::k32x32: return Shape<32, 32>::kSmem;
-    case BlockShape::k64x32: return Shape<64, 32>::kSmem;
+    case BlockShape::k32x16: return kWarpsPerCta * WarpMem<16>::kBytes;
+    case BlockShape::k32x32: return kWarpsPerCta * WarpMem<32>::kBytes;
+    case BlockShape::k32x64: return kWarpsPerCta * WarpMem<64>::kBytes;
   }
   return 0;
 }
 
-void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
-  switch (shape) {
-    case BlockShape::k32x16: bx = 32; by = 16; return;
-    case BlockShape::k32x32: bx = 32; by = 32; return;
-    case BlockShape::k64x32: bx = 64; by = 32; return;
-  }
-  bx = by = 0;
-}
+int tick_threads(BlockShape) { return kCtaThreads; }
 
-template <int BX, int BY>
-static const void* tick_fn(bool fixed, bool manning) {
-  if (fixed) return manning ? (const void*)tick_kernel<true, true, BX, BY> : (const void*)tick_kernel<true, false, BX, BY>;
-  return manning ? (const void*)tick_kernel<false, true, BX, BY> : (const void*)tick_kernel<false, false, BX, BY>;
+void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
+  bx = kStrip;
+  switch (shape) {
+    case BlockShape::k32x16: by = 16; return;
+    case BlockShape::k32x32: by = 32; return;
+    case BlockShape::k32x64: by = 64; return;
+  }
+  by = 0;
 }
 
 int tick_occupancy(BlockShape shape, bool fixed, bool manning) {
   const void* fn = nullptr;
-  size_t smem = tick_smem_bytes(shape);
   switch (shape) {
-    case BlockShape::k32x16: fn = tick_fn<32, 16>(fixed, manning); break;
-    case BlockShape::k32x32: fn = tick_fn<32, 32>(fixed, manning); break;
-    case BlockShape::k64x32: fn = tick_fn<64, 32>(fixed, manning); break;
+    case BlockShape::k32x16: fn = tick_fn<16>(fixed, manning); break;
+    case BlockShape::k32x32: fn = tick_fn<32>(fixed, manning); break;
+    case BlockShape::k32x64: fn = tick_fn<64>(fixed, manning); break;
   }
+  const size_t smem = tick_smem_bytes(shape);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
     return 0;
   int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kThreads, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCtaThreads, smem) != cudaSuccess)
     return 0;
   return blocks;
 }
@@ -716,16 +814,9 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning) {
 cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickArgs& a, int grid,
                         cudaStream_t s) {
   switch (shape) {
-#define WLC_TICK(BX, BY)                                                          \
-  case BlockShape::k##BX##x##BY:                                                  \
-    if (fixed) return manning ? Launch<BX, BY>::tick<true, true>(a, grid, s)      \
-                              : Launch<BX, BY>::tick<true, false>(a, grid, s);    \
-    return manning ? Launch<BX, BY>::tick<false, true>(a, grid, s)                \
-                   : Launch<BX, BY>::tick<false, false>(a, grid, s);
-    WLC_TICK(32, 16)
-    WLC_TICK(32, 32)
-    WLC_TICK(64, 32)
-#undef WLC_TICK
+    case BlockShape::k32x16: return tick_launch<16>(fixed, manning, a, grid, s);
+    case BlockShape::k32x32: return tick_launch<32>(fixed, manning, a, grid, s);
+    case BlockShape::k32x64: return tick_launch<64>(fixed, manning, a, grid, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -733,29 +824,18 @@ cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickAr
 cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaStream_t s) {
   if (a.n_items == 0) return cudaSuccess;
   switch (shape) {
-#define WLC_PRIME(BX, BY)                                                        \
-  case BlockShape::k##BX##x##BY:                                                 \
-    if (fixed) prime_kernel<true, BX, BY><<<a.n_items, kThreads, 0, s>>>(a);     \
-    else prime_kernel<false, BX, BY><<<a.n_items, kThreads, 0, s>>>(a);          \
-    return cudaGetLastError();
-    WLC_PRIME(32, 16)
-    WLC_PRIME(32, 32)
-    WLC_PRIME(64, 32)
-#undef WLC_PRIME
+    case BlockShape::k32x16: return prime_launch<16>(fixed, a, s);
+    case BlockShape::k32x32: return prime_launch<32>(fixed, a, s);
+    case BlockShape::k32x64: return prime_launch<64>(fixed, a, s);
   }
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_length_pass(bool fixed, const TileDesc* tiles, uint32_t tile, float max_dt,
                                cudaStream_t s) {
-  if (fixed) length_pass_kernel<true><<<1, kThreads, 0, s>>>(tiles, tile, max_dt);
-  else length_pass_kernel<false><<<1, kThreads, 0, s>>>(tiles, tile, max_dt);
+  if (fixed) length_pass_kernel<true><<<1, 256, 0, s>>>(tiles, tile, max_dt);
+  else length_pass_kernel<false><<<1, 256, 0, s>>>(tiles, tile, max_dt);
   return cudaGetLastError();
-}
-
-static int grid_for(size_t n) {
-  const size_t b = (n + 255) / 256;
-  return int(b < 4096 ? (b == 0 ? 1 : b) : 4096);
 }
 
 cudaError_t launch_write_state(TileDesc* tiles, uint32_t tile, size_t n, const double* h,

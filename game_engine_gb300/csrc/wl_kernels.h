@@ -20,11 +20,13 @@ struct TickArgs {
   float max_dt;
 };
 
-// The block of cells one work item steps. 32 x 32 is the default; the batched form's autotuner
+// The block of cells one work item steps (32 columns by 16, 32 or 64 rows; 8 threads a row of
+// four). 32 x 32 is the default; the batched form's autotuner
 // chooses among all three.
-enum class BlockShape : uint8_t { k32x16 = 0, k32x32 = 1, k64x32 = 2 };
+enum class BlockShape : uint8_t { k32x16 = 0, k32x32 = 1, k32x64 = 2 };
 
 size_t tick_smem_bytes(BlockShape shape);
+int tick_threads(BlockShape shape);
 void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by);
 // Sets the kernels' shared-memory opt-in on the current device and returns the resident CTAs per
 // SM (0 on an error).

@@ -1,0 +1,94 @@
+"""The C ABI without a device: every symbol include/wlcuda.h declares is exported, the mirrored
+structs keep the reference's sizes and offsets, the hash is FNV-1a, and a handle that was never
+created refuses every call (water_live_tests.cpp:22-55).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+
+from game_engine_gb300 import _abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PINS = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_pins.json")))
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(wl\w*)\s*\(", text))
+    return names
+
+
+def test_every_declared_symbol_is_exported(wl_lib):
+    names = declared_symbols()
+    assert len(names) >= 20
+    missing = [n for n in sorted(names) if not hasattr(wl_lib, n)]
+    assert not missing, missing
+    # and the Python declarations cover them
+    assert names <= set(_abi.SIGNATURES), sorted(names - set(_abi.SIGNATURES))
+
+
+def test_sizes_and_offsets_are_the_reference_s():
+    assert C.sizeof(_abi.StepParams) == PINS["sizes"]["StepParams"]
+    assert C.sizeof(_abi.Partial) == PINS["sizes"]["WaterPartial"]
+    assert C.sizeof(_abi.LedgerBits) == PINS["sizes"]["WaterLedger"]
+    off = PINS["offsets"]
+    for key, want in off.items():
+        if key == "source":
+            continue
+        struct, field = key.split(".")
+        cls = {"StepParams": _abi.StepParams, "WaterPartial": _abi.Partial,
+               "WaterLedger": _abi.LedgerBits}[struct]
+        assert getattr(cls, field).offset == want, key
+
+
+def test_hash_is_fnv1a_over_float_bytes(wl_lib, oracle_mod):
+    assert wl_lib.wl_hash_floats(None, 0) == int(PINS["fnv_empty"]["hash"])
+    rng = np.random.default_rng(7)
+    v = rng.standard_normal(1001).astype(np.float32)
+    p = v.ctypes.data_as(C.POINTER(C.c_float))
+    assert wl_lib.wl_hash_floats(p, v.size) == oracle_mod.hash_floats(v)
+    w = v.copy()
+    w.view(np.uint32)[500] ^= 1
+    assert wl_lib.wl_hash_floats(w.ctypes.data_as(C.POINTER(C.c_float)), w.size) != \
+        wl_lib.wl_hash_floats(p, v.size)
+
+
+def test_a_step_never_created_refuses_every_call(wl_lib):
+    # water_live_tests.cpp:38-47; WL_ERR_INVALID = 1, and 0 for the uint64 calls.
+    from game_engine_gb300 import water_live as wl
+    step = wl.DeviceStep()
+    one = np.zeros(1)
+    assert not step.valid()
+    assert not step.set_bed(one, 0.0)
+    assert not step.run_steps(1, 1.0)
+    assert step.advance(1.0) == 0
+    assert step.state_hash() == 0
+    err = C.create_string_buffer(128)
+    assert wl_lib.wl_valid(None) == 0
+    assert wl_lib.wl_run_steps(None, 1, 1.0, err, 128) == 1
+    assert b"no device" in err.value
+    assert wl_lib.wl_write_state(None, None, None, None, 0, err, 128) == 1
+    assert wl_lib.wl_read_ledger(None, None, err, 128) == 1
+    assert wl_lib.wl_enqueue_steps(None, None, 1, 1.0) == 1
+    assert wl_lib.wl_cell_count(None) == 0
+    wl_lib.wl_destroy(None)
+
+
+def test_an_empty_grid_is_refused(wl_lib):
+    # water_live.cpp:108, before any device is touched
+    cfg = _abi.Config(0, 4, 1.0, 9.81, 0.45, 1e-9, 0, 0, 0, 0, 0)
+    out = C.c_void_p()
+    err = C.create_string_buffer(128)
+    assert wl_lib.wl_create(C.byref(cfg), None, C.byref(out), err, 128) == 2
+    assert b"empty grid" in err.value
+    assert not out.value

@@ -1,0 +1,93 @@
+"""record() on a caller's stream and into a CUDA graph; the benchmark workloads at full size.
+
+Every per-tick quantity lives on the device, so a captured graph of tick launches replays
+correctly any number of times. At the benchmark's full sizes the oracle checks the first ticks bit
+for bit and the whole run is held to size-independent properties: the same bytes twice, and the
+water's balance.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cases
+from pairs import assert_same, make_pair
+from game_engine_gb300 import water_live as wl, workloads
+
+pytestmark = pytest.mark.gpu
+INF = float("inf")
+
+
+def test_enqueue_on_a_caller_stream(gpu):
+    import torch
+    s = cases.slope(False)
+    dev, ref = make_pair(s)
+    stream = torch.cuda.Stream()
+    assert dev.record(stream.cuda_stream, 37, INF)
+    stream.synchronize()
+    ref.run_steps(37, INF)
+    assert_same(dev, ref, "caller stream")
+
+
+def test_graph_capture_replays(gpu):
+    import torch
+    s = cases.slope(False)
+    dev, ref = make_pair(s)
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        assert dev.record(torch.cuda.current_stream().cuda_stream, 5, INF)
+    # Capture records the launches without running them; each replay is five ticks, and a
+    # replay of an odd count flips the copy on the device, where every launch reads it.
+    for _ in range(7):
+        graph.replay()
+    torch.cuda.synchronize()
+    ref.run_steps(35, INF)
+    assert_same(dev, ref, "graph replays")
+
+
+def tile_case(t):
+    return dict(nx=t.nx, ny=t.ny, cell_m=t.cell_m, bed=t.bed, h=t.h, source=t.source)
+
+
+def test_plain_256_thousand_ticks_hash(gpu):
+    # The plain configuration: 256 x 256 fBm, a 2 m column, 1000 ticks at max_dt 0.01 s.
+    t = workloads.plain_256()
+    dev, ref = make_pair(tile_case(t))
+    assert dev.run_steps(1000, 0.01)
+    ref.run_steps(1000, 0.01)
+    assert_same(dev, ref, "plain_256")
+
+
+def test_plain_2048_first_ticks_bit_exact(gpu):
+    t = workloads.plain_2048()
+    dev, ref = make_pair(tile_case(t))
+    assert dev.run_steps(3, 0.01)
+    ref.run_steps(3, 0.01)
+    assert_same(dev, ref, "plain_2048, 3 ticks")
+
+
+def test_plain_2048_full_run_properties(gpu):
+    # 500 ticks of rain: the same bytes twice, and the ledger's balance of the water.
+    from pairs import config
+    t = workloads.plain_2048()
+    c = tile_case(t)
+    hashes = []
+    for _ in range(2):
+        dev = wl.DeviceStep()
+        assert dev.create(config(c)), dev.error
+        assert dev.set_bed(c["bed"]) and dev.set_source(c["source"])
+        assert dev.write_state(c["h"], np.zeros(t.cells), np.zeros(t.cells))
+        h0 = dev.read_state()[0]
+        assert dev.run_steps(500, 0.01)
+        hashes.append(dev.state_hash())
+    assert hashes[0] == hashes[1] != 0
+    h = dev.read_state()[0]
+    led = dev.read_ledger()
+    assert led["steps"] == 500
+    before = h0.sum()
+    after = h.sum()
+    balance = after - before - led["source_m3"] - led["roundoff_m3"]
+    involved = before + abs(led["source_m3"])
+    assert abs(balance) <= 500 * 2.0 ** -24 * involved
+    assert led["source_m3"] > 0
