@@ -55,6 +55,19 @@ class Ledger(C.Structure):
                 ("remaining_s", C.c_double), ("steps", C.c_uint64)]
 
 
+class Tile(C.Structure):
+    """wl_tile: one tile of a batch."""
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("west_open", C.c_uint8),
+                ("east_open", C.c_uint8), ("south_open", C.c_uint8), ("north_open", C.c_uint8)]
+
+
+class Tuning(C.Structure):
+    """wl_tuning: the batched launch's shape."""
+    _fields_ = [("block_rows", C.c_uint32), ("order", C.c_uint32), ("us_per_tick", C.c_float)]
+
+
+_u64p = C.POINTER(C.c_uint64)
+
 # name -> (restype, argtypes); every symbol include/wlcuda.h declares.
 SIGNATURES = {
     "wl_create": (C.c_int, [C.POINTER(Config), C.POINTER(Options), C.POINTER(C.c_void_p), *_err]),
@@ -80,6 +93,30 @@ SIGNATURES = {
     "wl_step_stream": (wl_stream, [C.c_void_p]),
     "wl_write_state_device": (C.c_int, [C.c_void_p, C.c_void_p, wl_stream]),
     "wl_device_planes": (C.c_int, [C.c_void_p, C.POINTER(_fp), C.POINTER(_fp), *_err]),
+    "wl_batch_create": (C.c_int, [C.POINTER(Config), C.POINTER(Options), C.POINTER(Tile),
+                                  C.c_uint32, C.POINTER(C.c_void_p), *_err]),
+    "wl_batch_destroy": (None, [C.c_void_p]),
+    "wl_batch_tile_count": (C.c_uint32, [C.c_void_p]),
+    "wl_batch_cell_count": (C.c_uint64, [C.c_void_p]),
+    "wl_batch_tile_first": (C.c_uint64, [C.c_void_p, C.c_uint32]),
+    "wl_batch_write_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
+    "wl_batch_set_bed": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_double, *_err]),
+    "wl_batch_set_manning": (C.c_int, [C.c_void_p, _dp, C.c_size_t, *_err]),
+    "wl_batch_set_source": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_uint32, C.c_int, *_err]),
+    "wl_batch_enqueue_ticks": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32, C.c_float]),
+    "wl_batch_run_ticks": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_int, *_err]),
+    "wl_batch_enqueue_tile_tick": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32, C.c_float]),
+    "wl_batch_run_tile_ticks": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_int, *_err]),
+    "wl_batch_read_tile_bits": (C.c_int, [C.c_void_p, C.c_uint32, _fp, C.c_size_t, *_err]),
+    "wl_batch_read_all_bits": (C.c_int, [C.c_void_p, _fp, C.c_size_t, *_err]),
+    "wl_batch_tile_hash": (C.c_uint64, [C.c_void_p, C.c_uint32, *_err]),
+    "wl_batch_tile_hashes": (C.c_int, [C.c_void_p, _u64p, C.c_uint32, *_err]),
+    "wl_batch_read_ledgers": (C.c_int, [C.c_void_p, C.POINTER(Ledger), C.c_uint32, *_err]),
+    "wl_batch_autotune": (C.c_int, [C.c_void_p, C.c_float, C.c_uint32, C.POINTER(Tuning), *_err]),
+    "wl_batch_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning), *_err]),
+    "wl_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "wl_batch_stream": (wl_stream, [C.c_void_p]),
+    "wl_util_fbm": (C.c_int, [_dp, C.c_uint32, C.c_uint32, C.c_double, C.c_uint64, C.c_uint32]),
 }
 
 

@@ -18,7 +18,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libwlcuda.so")
 
-SOURCES = ["wl_kernels.cu", "wl_adjoint.cu", "wl_tiles.cpp", "wl_api.cpp", "wl_batch.cpp"]
+SOURCES = ["wl_kernels.cu", "wl_adjoint.cu", "wl_tiles.cpp", "wl_api.cpp", "wl_batch.cpp",
+           "wl_util.cpp"]
 HEADERS = ["wl_device.cuh", "wl_kernels.h", "wl_tiles.h", "wl_adjoint.h", "wl_batch.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,7 +45,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     cc = nvcc()
-    headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "wlcuda.h")]
+    headers = [os.path.join(CSRC, h) for h in HEADERS] + [
+        os.path.join(ROOT, "include", h) for h in ("wlcuda.h", "wlcuda_util.h")]
     procs, objs = [], []
     for src in SOURCES:
         path = os.path.join(CSRC, src)

@@ -1,0 +1,526 @@
+// The batched form's C ABI (include/wlcuda.h, wl_batch_*): many tiles of uneven sizes stepped by
+// one persistent launch per tick, replayed from a captured CUDA graph, with the block shape and
+// the order work items are dealt in chosen by timing the candidates on the batch itself.
+#include "wlcuda.h"
+
+#include "wl_tiles.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <map>
+#include <mutex>
+#include <new>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+using wlc::BlockShape;
+using wlc::TileSet;
+
+struct wl_batch {
+  TileSet set;
+  wl_config common{};
+  wl_options options{};
+  std::vector<wlc::TileSpec> specs;
+  uint32_t flags = 0;  // the batch's Manning / source / compensate flags
+  uint32_t source_every = 1;
+  wl_tuning tuning{};
+  // The captured graph of `graph_ticks` ticks and what it was captured for.
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_ticks = 0;
+  float graph_max_dt = 0.0f;
+  uint64_t graph_key = 0;
+  cudaGraphExec_t tile_graph = nullptr;
+  float tile_graph_max_dt = 0.0f;
+  uint64_t tile_graph_key = 0;
+  ~wl_batch() {
+    if (graph != nullptr) cudaGraphExecDestroy(graph);
+    if (tile_graph != nullptr) cudaGraphExecDestroy(tile_graph);
+  }
+};
+
+namespace {
+
+int fail(char* err, size_t len, int code, const std::string& msg) {
+  if (err != nullptr && len > 0) {
+    const size_t k = msg.size() < len - 1 ? msg.size() : len - 1;
+    std::memcpy(err, msg.data(), k);
+    err[k] = '\0';
+  }
+  return code;
+}
+
+int cuda_fail(char* err, size_t len, const std::string& msg) {
+  const int code = msg.find("wait limit") != std::string::npos ? WL_ERR_TIMEOUT : WL_ERR_CUDA;
+  return fail(err, len, code, msg);
+}
+
+bool valid(const wl_batch* b) { return b != nullptr && b->set.valid(); }
+const char* k_no_device = "water_live: no device";
+
+BlockShape shape_of_rows(uint32_t rows) {
+  return rows == 16 ? BlockShape::k32x16 : rows == 64 ? BlockShape::k32x64 : BlockShape::k32x32;
+}
+
+// Work-item orders: 0 tiles by index, 1 the largest tiles first.
+std::vector<uint32_t> item_order(const std::vector<wlc::TileSpec>& specs, uint32_t order) {
+  std::vector<uint32_t> o(specs.size());
+  for (uint32_t i = 0; i < o.size(); ++i) o[i] = i;
+  if (order == 1)
+    std::stable_sort(o.begin(), o.end(), [&](uint32_t a, uint32_t b) {
+      return uint64_t(specs[a].nx) * specs[a].ny > uint64_t(specs[b].nx) * specs[b].ny;
+    });
+  return o;
+}
+
+// What a captured graph depends on: the block shape, the order, the launch's grid and variant.
+uint64_t launch_key(const wl_batch* b) {
+  return (uint64_t(b->set.shape()) << 48) ^ (uint64_t(b->tuning.order) << 40) ^
+         (uint64_t(b->set.grid()) << 8) ^ (b->set.any_manning() ? 1u : 0u);
+}
+
+void drop_graphs(wl_batch* b) {
+  if (b->graph != nullptr) cudaGraphExecDestroy(b->graph);
+  if (b->tile_graph != nullptr) cudaGraphExecDestroy(b->tile_graph);
+  b->graph = nullptr;
+  b->tile_graph = nullptr;
+  b->graph_ticks = 0;
+}
+
+// The tuning cache: one entry per (SM count, size histogram), kept for the process and, when
+// WLCUDA_TUNING_CACHE names a file, across processes.
+std::mutex g_cache_mu;
+std::map<std::string, wl_tuning> g_cache;
+
+std::string histogram_key(int sms, const std::vector<wlc::TileSpec>& specs, uint8_t fixed) {
+  std::map<std::pair<uint32_t, uint32_t>, uint32_t> hist;
+  for (const auto& s : specs) hist[{s.nx, s.ny}] += 1;
+  std::ostringstream k;
+  k << "sm" << sms << (fixed ? "/fixed" : "/native");
+  for (const auto& [size, count] : hist) k << "/" << size.first << "x" << size.second << ":" << count;
+  return k.str();
+}
+
+bool cache_lookup(const std::string& key, wl_tuning* out) {
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  auto it = g_cache.find(key);
+  if (it == g_cache.end()) {
+    const char* path = std::getenv("WLCUDA_TUNING_CACHE");
+    if (path == nullptr) return false;
+    std::ifstream f(path);
+    std::string line;
+    while (std::getline(f, line)) {
+      std::istringstream in(line);
+      std::string k;
+      wl_tuning t{};
+      if (in >> k >> t.block_rows >> t.order >> t.us_per_tick) g_cache[k] = t;
+    }
+    it = g_cache.find(key);
+    if (it == g_cache.end()) return false;
+  }
+  *out = it->second;
+  return true;
+}
+
+void cache_store(const std::string& key, const wl_tuning& t) {
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  g_cache[key] = t;
+  if (const char* path = std::getenv("WLCUDA_TUNING_CACHE")) {
+    std::ofstream f(path, std::ios::app);
+    f << key << " " << t.block_rows << " " << t.order << " " << t.us_per_tick << "\n";
+  }
+}
+
+bool time_ticks(wl_batch* b, uint32_t ticks, float max_dt, float* us, std::string* msg) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, b->set.stream());
+  const cudaError_t e = b->set.enqueue_ticks(b->set.stream(), ticks, max_dt);
+  cudaEventRecord(e1, b->set.stream());
+  bool ok = e == cudaSuccess && b->set.wait(msg);
+  float ms = 0.0f;
+  if (ok) ok = cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!ok && msg->empty()) *msg = "water_live: a trial tick failed";
+  *us = ms * 1000.0f / float(ticks);
+  return ok;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wl_batch_create(const wl_config* common, const wl_options* options, const wl_tile* tiles,
+                    uint32_t count, wl_batch** out, char* err, size_t err_len) {
+  if (out == nullptr || common == nullptr || tiles == nullptr)
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no config or tiles");
+  *out = nullptr;
+  if (count == 0) return fail(err, err_len, WL_ERR_SIZE, "water_live: no tiles");
+  auto* b = new (std::nothrow) wl_batch;
+  if (b == nullptr) return fail(err, err_len, WL_ERR_ALLOC, "water_live: out of host memory");
+  b->common = *common;
+  if (options != nullptr) b->options = *options;
+  b->specs.resize(count);
+  for (uint32_t i = 0; i < count; ++i) {
+    if (tiles[i].nx == 0 || tiles[i].ny == 0) {
+      delete b;
+      return fail(err, err_len, WL_ERR_SIZE, "water_live: an empty grid");
+    }
+    wlc::TileSpec& s = b->specs[i];
+    s.nx = tiles[i].nx;
+    s.ny = tiles[i].ny;
+    s.cell_m = common->cell_m;
+    s.gravity = common->gravity;
+    s.cfl = common->cfl;
+    s.dry_depth_m = common->dry_depth_m;
+    s.open_edges = (tiles[i].west_open ? 1u : 0u) | (tiles[i].east_open ? 2u : 0u) |
+                   (tiles[i].south_open ? 4u : 0u) | (tiles[i].north_open ? 8u : 0u);
+  }
+  b->tuning.block_rows = 32;
+  b->tuning.order = 1;
+  b->tuning.us_per_tick = 0.0f;
+  std::string msg;
+  if (!b->set.create(common->device, b->specs, b->options.ops == WL_OPS_FIXED,
+                     shape_of_rows(b->tuning.block_rows), item_order(b->specs, b->tuning.order),
+                     &msg)) {
+    delete b;
+    return cuda_fail(err, err_len, msg);
+  }
+  *out = b;
+  return WL_OK;
+}
+
+void wl_batch_destroy(wl_batch* b) { delete b; }
+
+uint32_t wl_batch_tile_count(const wl_batch* b) { return valid(b) ? b->set.tile_count() : 0u; }
+
+uint64_t wl_batch_cell_count(const wl_batch* b) { return valid(b) ? b->set.total_cells() : 0u; }
+
+uint64_t wl_batch_tile_first(const wl_batch* b, uint32_t tile) {
+  return valid(b) && tile < b->set.tile_count() ? b->set.first_cell(tile) : 0u;
+}
+
+int wl_batch_write_state(wl_batch* b, const double* h, const double* hu, const double* hv,
+                         size_t total, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (total != b->set.total_cells() || h == nullptr || hu == nullptr || hv == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: states that do not fit the tiles");
+  std::string msg;
+  if (!b->set.write_all(h, hu, hv, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_batch_set_bed(wl_batch* b, const double* bed, size_t total, double datum, char* err,
+                     size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (total != b->set.total_cells() || bed == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: beds that do not fit the tiles");
+  std::string msg;
+  if (!b->set.set_plane_all(0, bed, datum, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_batch_set_manning(wl_batch* b, const double* manning, size_t total, char* err,
+                         size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  std::string msg;
+  if (total == 0) {
+    b->flags &= ~WL_FLAG_MANNING;
+    if (!b->set.set_flags_all(0u, WL_FLAG_MANNING, b->source_every, false, &msg))
+      return cuda_fail(err, err_len, msg);
+    drop_graphs(b);
+    return WL_OK;
+  }
+  if (total != b->set.total_cells() || manning == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a Manning's n that does not fit");
+  if (!b->set.set_plane_all(1, manning, 0.0, &msg) ||
+      !b->set.set_flags_all(WL_FLAG_MANNING, 0u, b->source_every, false, &msg))
+    return cuda_fail(err, err_len, msg);
+  b->flags |= WL_FLAG_MANNING;
+  drop_graphs(b);
+  return WL_OK;
+}
+
+int wl_batch_set_source(wl_batch* b, const double* source, size_t total, uint32_t every,
+                        int compensate, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  b->source_every = every == 0 ? 1 : every;
+  const uint32_t comp = compensate ? WL_FLAG_COMPENSATE : 0u;
+  std::string msg;
+  if (total == 0) {
+    if (!b->set.set_flags_all(comp, WL_FLAG_SOURCE | (comp ? 0u : WL_FLAG_COMPENSATE),
+                              b->source_every, true, &msg))
+      return cuda_fail(err, err_len, msg);
+    drop_graphs(b);
+    return WL_OK;
+  }
+  if (total != b->set.total_cells() || source == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a source that does not fit");
+  if (!b->set.set_plane_all(2, source, 0.0, &msg) ||
+      !b->set.set_flags_all(WL_FLAG_SOURCE | comp, comp ? 0u : WL_FLAG_COMPENSATE,
+                            b->source_every, true, &msg))
+    return cuda_fail(err, err_len, msg);
+  drop_graphs(b);
+  return WL_OK;
+}
+
+int wl_batch_enqueue_ticks(wl_batch* b, wl_stream stream, uint32_t count, float max_dt) {
+  if (!valid(b)) return WL_ERR_INVALID;
+  if (cudaSetDevice(b->set.device()) != cudaSuccess) return WL_ERR_CUDA;
+  cudaStream_t st = stream == nullptr ? b->set.stream() : reinterpret_cast<cudaStream_t>(stream);
+  return b->set.enqueue_ticks(st, count, max_dt) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
+}
+
+int wl_batch_run_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph, char* err,
+                       size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (cudaSetDevice(b->set.device()) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
+  cudaStream_t st = b->set.stream();
+  uint32_t left = count;
+  if (use_graph && count > 0) {
+    // One captured graph of up to 16 ticks (each a single persistent launch), replayed.
+    const uint32_t g = count < 16 ? count : 16;
+    const uint64_t key = launch_key(b);
+    if (b->graph == nullptr || b->graph_ticks != g || b->graph_max_dt != max_dt ||
+        b->graph_key != key) {
+      if (b->graph != nullptr) cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaStreamBeginCapture");
+      const cudaError_t e = b->set.enqueue_ticks(st, g, max_dt);
+      const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+      if (e != cudaSuccess || e2 != cudaSuccess ||
+          cudaGraphInstantiate(&b->graph, graph, 0) != cudaSuccess) {
+        if (graph != nullptr) cudaGraphDestroy(graph);
+        b->graph = nullptr;
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: the tick graph could not be made");
+      }
+      cudaGraphDestroy(graph);
+      b->graph_ticks = g;
+      b->graph_max_dt = max_dt;
+      b->graph_key = key;
+    }
+    while (left >= b->graph_ticks) {
+      if (cudaGraphLaunch(b->graph, st) != cudaSuccess)
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaGraphLaunch");
+      left -= b->graph_ticks;
+    }
+  }
+  if (left > 0 && b->set.enqueue_ticks(st, left, max_dt) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: the tick");
+  std::string msg;
+  if (!b->set.wait(&msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_batch_enqueue_tile_tick(wl_batch* b, wl_stream stream, uint32_t tile, float max_dt) {
+  if (!valid(b)) return WL_ERR_INVALID;
+  if (tile >= b->set.tile_count()) return WL_ERR_ARGUMENT;
+  if (cudaSetDevice(b->set.device()) != cudaSuccess) return WL_ERR_CUDA;
+  cudaStream_t st = stream == nullptr ? b->set.stream() : reinterpret_cast<cudaStream_t>(stream);
+  return b->set.enqueue_tile_tick(st, tile, max_dt) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
+}
+
+int wl_batch_run_tile_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph, char* err,
+                            size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (cudaSetDevice(b->set.device()) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
+  cudaStream_t st = b->set.stream();
+  const uint32_t n = b->set.tile_count();
+  if (use_graph) {
+    const uint64_t key = launch_key(b);
+    if (b->tile_graph == nullptr || b->tile_graph_max_dt != max_dt || b->tile_graph_key != key) {
+      if (b->tile_graph != nullptr) cudaGraphExecDestroy(b->tile_graph);
+      b->tile_graph = nullptr;
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaStreamBeginCapture");
+      cudaError_t e = cudaSuccess;
+      for (uint32_t t = 0; t < n && e == cudaSuccess; ++t) e = b->set.enqueue_tile_tick(st, t, max_dt);
+      const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+      if (e != cudaSuccess || e2 != cudaSuccess ||
+          cudaGraphInstantiate(&b->tile_graph, graph, 0) != cudaSuccess) {
+        if (graph != nullptr) cudaGraphDestroy(graph);
+        b->tile_graph = nullptr;
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: the per-tile graph could not be made");
+      }
+      cudaGraphDestroy(graph);
+      b->tile_graph_max_dt = max_dt;
+      b->tile_graph_key = key;
+    }
+    for (uint32_t k = 0; k < count; ++k)
+      if (cudaGraphLaunch(b->tile_graph, st) != cudaSuccess)
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaGraphLaunch");
+  } else {
+    for (uint32_t k = 0; k < count; ++k)
+      for (uint32_t t = 0; t < n; ++t)
+        if (b->set.enqueue_tile_tick(st, t, max_dt) != cudaSuccess)
+          return fail(err, err_len, WL_ERR_CUDA, "water_live: a tile's tick");
+  }
+  std::string msg;
+  if (!b->set.wait(&msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_batch_read_tile_bits(wl_batch* b, uint32_t tile, float* planes, size_t count, char* err,
+                            size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (tile >= b->set.tile_count() || planes == nullptr ||
+      count != size_t(WL_STATE_PLANES) * b->set.cells(tile))
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: planes of the wrong size");
+  std::string msg;
+  if (!b->set.read_state_bits(tile, planes, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_batch_read_all_bits(wl_batch* b, float* planes, size_t count, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (planes == nullptr || count != size_t(WL_STATE_PLANES) * b->set.total_cells())
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: planes of the wrong size");
+  std::string msg;
+  if (!b->set.read_all_bits(planes, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_batch_tile_hashes(wl_batch* b, uint64_t* out, uint32_t count, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (out == nullptr || count != b->set.tile_count())
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: hashes of the wrong count");
+  std::vector<float> all;
+  try {
+    all.resize(size_t(WL_STATE_PLANES) * b->set.total_cells());
+  } catch (...) {
+    return fail(err, err_len, WL_ERR_ALLOC, "water_live: out of host memory");
+  }
+  std::string msg;
+  if (!b->set.read_all_bits(all.data(), &msg)) return cuda_fail(err, err_len, msg);
+  // FNV-1a is a sequence: each tile's hash is one pass; the tiles go to the host's threads.
+  const uint32_t threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> pool;
+  for (uint32_t w = 0; w < threads; ++w)
+    pool.emplace_back([&, w] {
+      for (uint32_t t = w; t < count; t += threads)
+        out[t] = wlc::fnv1a_floats(all.data() + size_t(WL_STATE_PLANES) * b->set.first_cell(t),
+                                   size_t(WL_STATE_PLANES) * b->set.cells(t));
+    });
+  for (auto& th : pool) th.join();
+  return WL_OK;
+}
+
+uint64_t wl_batch_tile_hash(wl_batch* b, uint32_t tile, char* err, size_t err_len) {
+  if (!valid(b)) {
+    fail(err, err_len, WL_ERR_INVALID, k_no_device);
+    return 0;
+  }
+  if (tile >= b->set.tile_count()) {
+    fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no such tile");
+    return 0;
+  }
+  std::vector<float> planes(size_t(WL_STATE_PLANES) * b->set.cells(tile));
+  std::string msg;
+  if (!b->set.read_state_bits(tile, planes.data(), &msg)) {
+    cuda_fail(err, err_len, msg);
+    return 0;
+  }
+  return wlc::fnv1a_floats(planes.data(), planes.size());
+}
+
+int wl_batch_read_ledgers(wl_batch* b, wl_ledger* out, uint32_t count, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (out == nullptr || count != b->set.tile_count())
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: ledgers of the wrong count");
+  std::vector<wlc::TileCtl> ctl(count);
+  std::string msg;
+  if (!b->set.flush_all(&msg) || !b->set.read_all_ctl(ctl.data(), &msg))
+    return cuda_fail(err, err_len, msg);
+  for (uint32_t t = 0; t < count; ++t) {
+    const wlc::LedgerBits& l = ctl[t].ledger;
+    out[t].source_m3 = double(l.source_hi) + double(l.source_lo);
+    out[t].open_edge_out_m3 = double(l.open_hi) + double(l.open_lo);
+    out[t].roundoff_m3 = double(l.roundoff_hi) + double(l.roundoff_lo);
+    out[t].time_s = double(l.time_hi) + double(l.time_lo);
+    out[t].remaining_s = double(l.remaining_s);
+    out[t].steps = l.steps;
+  }
+  return WL_OK;
+}
+
+int wl_batch_set_tuning(wl_batch* b, const wl_tuning* t, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (t == nullptr || (t->block_rows != 16 && t->block_rows != 32 && t->block_rows != 64) ||
+      t->order > 1)
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: a tuning out of range");
+  std::string msg;
+  if (!b->set.reshape(shape_of_rows(t->block_rows), item_order(b->specs, t->order), &msg))
+    return cuda_fail(err, err_len, msg);
+  b->tuning = *t;
+  drop_graphs(b);
+  return WL_OK;
+}
+
+int wl_batch_get_tuning(const wl_batch* b, wl_tuning* out) {
+  if (!valid(b) || out == nullptr) return WL_ERR_INVALID;
+  *out = b->tuning;
+  return WL_OK;
+}
+
+int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning* chosen,
+                      char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (cudaSetDevice(b->set.device()) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->set.device());
+  const std::string key = histogram_key(sms, b->specs, b->options.ops);
+  wl_tuning best{};
+  std::string msg;
+  if (!cache_lookup(key, &best)) {
+    if (trial_ticks == 0) trial_ticks = 4;
+    // Trials run on the batch's own state and are undone: a snapshot of everything a tick
+    // writes is taken first and put back after.
+    if (!b->set.snapshot(&msg)) return cuda_fail(err, err_len, msg);
+    best.us_per_tick = std::numeric_limits<float>::infinity();
+    for (uint32_t rows : {16u, 32u, 64u}) {
+      for (uint32_t order : {0u, 1u}) {
+        if (!b->set.reshape(shape_of_rows(rows), item_order(b->specs, order), &msg) ||
+            !b->set.restore(&msg))
+          return cuda_fail(err, err_len, msg);
+        float warm = 0.0f, us = 0.0f;
+        if (!time_ticks(b, 1, max_dt, &warm, &msg) || !b->set.restore(&msg) ||
+            !time_ticks(b, trial_ticks, max_dt, &us, &msg))
+          return cuda_fail(err, err_len, msg);
+        if (us < best.us_per_tick) {
+          best.block_rows = rows;
+          best.order = order;
+          best.us_per_tick = us;
+        }
+      }
+    }
+    if (!b->set.restore(&msg)) return cuda_fail(err, err_len, msg);
+    b->set.drop_snapshot();
+    cache_store(key, best);
+  }
+  if (!b->set.reshape(shape_of_rows(best.block_rows), item_order(b->specs, best.order), &msg))
+    return cuda_fail(err, err_len, msg);
+  b->tuning = best;
+  drop_graphs(b);
+  if (chosen != nullptr) *chosen = best;
+  return WL_OK;
+}
+
+wl_stream wl_batch_stream(wl_batch* b) {
+  return valid(b) ? reinterpret_cast<wl_stream>(b->set.stream()) : nullptr;
+}
+
+}  // extern "C"

@@ -736,6 +736,82 @@ __global__ void copy_state_kernel(const TileDesc* tiles, uint32_t tile, float* d
     dst[i] = p[i];
 }
 
+// ---- whole batches: arrays of every tile's cells, tile after tile ------------------------------
+
+// The tile holding global cell index k of the batch (first[t] = the tile's first cell).
+__device__ __forceinline__ uint32_t tile_of_cell(const uint64_t* first, uint32_t count, uint64_t k) {
+  uint32_t lo = 0, hi = count;
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (first[mid] <= k) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// write_state for every tile at once from concatenated doubles (water_live.cpp:276-282).
+__global__ void scatter_state_kernel(TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                     uint64_t total, const double* h, const double* hu,
+                                     const double* hv) {
+  for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t t = tile_of_cell(first, count, k);
+    const TileDesc& T = tiles[t];
+    const size_t n = size_t(T.nx) * T.ny;
+    const size_t i = size_t(k - first[t]);
+    float* p = T.state[T.ctl->cur];
+    p[i] = __double2float_rn(h[k]);
+    p[n + i] = __double2float_rn(hu[k]);
+    p[2 * n + i] = __double2float_rn(hv[k]);
+    p[3 * n + i] = 0.0f;
+    if (i == 0) reset_ledger(T.ctl);
+  }
+}
+
+// set_bed / set_manning / set_source for every tile at once: which 0 bed, 1 Manning, 2 source.
+__global__ void scatter_plane_kernel(TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                     uint64_t total, const double* v, double datum, int which) {
+  for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t t = tile_of_cell(first, count, k);
+    const TileDesc& T = tiles[t];
+    float* dst = const_cast<float*>(which == 0 ? T.bed : which == 1 ? T.manning : T.source);
+    dst[k - first[t]] = __double2float_rn(v[k] - datum);
+  }
+}
+
+// Every tile's current copy, all four planes, tile after tile (4 n floats a tile).
+__global__ void gather_state_kernel(const TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                    uint64_t total, float* dst) {
+  for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+       k += uint64_t(gridDim.x) * blockDim.x) {
+    const uint32_t t = tile_of_cell(first, count, k);
+    const TileDesc& T = tiles[t];
+    const size_t n = size_t(T.nx) * T.ny;
+    const size_t i = size_t(k - first[t]);
+    const float* p = T.state[T.ctl->cur];
+    float* d = dst + 4 * first[t];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) d[q * n + i] = p[q * n + i];
+  }
+}
+
+// A flush of every tile at once: a CTA a tile, dt_main with max_dt 0 (slang:412-479).
+template <bool FIXED>
+__global__ void __launch_bounds__(256) flush_all_kernel(const TileDesc* tiles) {
+  __shared__ float s[3 * kGroupCells];
+  __shared__ uint32_t s_ab[2];
+  const TileDesc& T = tiles[blockIdx.x];
+  Partial* rec = T.rec[T.ctl->rec];
+  fold_cta(rec, T.groups_x * T.groups_y, s, s_ab);
+  if (threadIdx.x == 0) {
+    LedgerBits l = T.ctl->ledger;
+    ledger_update<FIXED>(l, s[0], s[kGroupCells], s[2 * kGroupCells], __uint_as_float(s_ab[0]),
+                         __uint_as_float(s_ab[1]), T.cfl, T.cell_m, 0.0f);
+    T.ctl->ledger = l;
+  }
+}
+
 template <int H>
 const void* tick_fn(bool fixed, bool manning) {
   if (fixed)
@@ -864,6 +940,33 @@ cudaError_t launch_read_state(const TileDesc* tiles, uint32_t tile, size_t n, do
 cudaError_t launch_copy_state(const TileDesc* tiles, uint32_t tile, size_t n, float* dst,
                               cudaStream_t s) {
   copy_state_kernel<<<grid_for(4 * n), 256, 0, s>>>(tiles, tile, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_state(TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                 uint64_t total, const double* h, const double* hu,
+                                 const double* hv, cudaStream_t s) {
+  scatter_state_kernel<<<grid_for(total), 256, 0, s>>>(tiles, count, first, total, h, hu, hv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_plane(TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                 uint64_t total, const double* v, double datum, int which,
+                                 cudaStream_t s) {
+  scatter_plane_kernel<<<grid_for(total), 256, 0, s>>>(tiles, count, first, total, v, datum, which);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_state(const TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                uint64_t total, float* dst, cudaStream_t s) {
+  gather_state_kernel<<<grid_for(total), 256, 0, s>>>(tiles, count, first, total, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flush_all(bool fixed, const TileDesc* tiles, uint32_t count, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  if (fixed) flush_all_kernel<true><<<count, 256, 0, s>>>(tiles);
+  else flush_all_kernel<false><<<count, 256, 0, s>>>(tiles);
   return cudaGetLastError();
 }
 

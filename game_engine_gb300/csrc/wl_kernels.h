@@ -48,4 +48,18 @@ cudaError_t launch_read_state(const TileDesc* tiles, uint32_t tile, size_t n, do
 cudaError_t launch_copy_state(const TileDesc* tiles, uint32_t tile, size_t n, float* dst,
                               cudaStream_t s);
 
+// Whole batches: arrays hold every tile's cells tile after tile; first[t] is tile t's first cell.
+cudaError_t launch_scatter_state(TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                 uint64_t total, const double* h, const double* hu,
+                                 const double* hv, cudaStream_t s);
+// which: 0 the bed (less `datum`), 1 Manning's n, 2 the source.
+cudaError_t launch_scatter_plane(TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                 uint64_t total, const double* v, double datum, int which,
+                                 cudaStream_t s);
+// Every tile's current copy, four planes a tile (4 * first[t] floats before tile t).
+cudaError_t launch_gather_state(const TileDesc* tiles, uint32_t count, const uint64_t* first,
+                                uint64_t total, float* dst, cudaStream_t s);
+// A flush (dt_main with max_dt 0) of every tile.
+cudaError_t launch_flush_all(bool fixed, const TileDesc* tiles, uint32_t count, cudaStream_t s);
+
 }  // namespace wlc

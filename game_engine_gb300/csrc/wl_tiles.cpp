@@ -73,6 +73,12 @@ void TileSet::destroy() {
   }
   if (base_ != nullptr) cudaFree(base_);
   if (staging_ != nullptr) cudaFree(staging_);
+  if (snap_ != nullptr) cudaFree(snap_);
+  if (d_item_tile_ != nullptr) cudaFree(d_item_tile_);
+  snap_ = nullptr;
+  d_first_ = nullptr;
+  first_.clear();
+  mutable_bytes_ = 0;
   stream_ = nullptr;
   base_ = nullptr;
   staging_ = nullptr;
@@ -116,26 +122,38 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
     destroy();
     return false;
   }
-  // One allocation: per tile the planes and records, then the control blocks and descriptors.
+  // One allocation. First what a tick writes (every tile's two state copies and two record
+  // buffers, then the control blocks), so a snapshot is one copy; then the inputs (bed, Manning's
+  // n, source), the descriptors, the cell offsets and the work counter.
   const size_t nt = tiles.size();
   std::vector<size_t> off_state(nt), off_inputs(nt), off_rec(nt);
   size_t total = 0;
   total_cells_ = 0;
+  first_.assign(nt, 0);
   for (size_t i = 0; i < nt; ++i) {
     const size_t n = size_t(tiles[i].nx) * tiles[i].ny;
-    const size_t groups = size_t((tiles[i].nx + 15) / 16) * ((tiles[i].ny + 15) / 16);
+    first_[i] = total_cells_;
     total_cells_ += n;
     off_state[i] = total;
     total += 2 * align_up(kStatePlanes * n * sizeof(float));
-    off_inputs[i] = total;
-    total += 3 * align_up(n * sizeof(float));
+  }
+  for (size_t i = 0; i < nt; ++i) {
+    const size_t groups = size_t((tiles[i].nx + 15) / 16) * ((tiles[i].ny + 15) / 16);
     off_rec[i] = total;
     total += 2 * align_up(groups * sizeof(Partial));
   }
   const size_t off_ctl = total;
   total += align_up(nt * sizeof(TileCtl));
+  mutable_bytes_ = total;
+  for (size_t i = 0; i < nt; ++i) {
+    const size_t n = size_t(tiles[i].nx) * tiles[i].ny;
+    off_inputs[i] = total;
+    total += 3 * align_up(n * sizeof(float));
+  }
   const size_t off_desc = total;
   total += align_up(nt * sizeof(TileDesc));
+  const size_t off_first = total;
+  total += align_up(nt * sizeof(uint64_t));
   const size_t off_work = total;
   total += align_up(sizeof(WorkCtl));
   if (!check(cudaMalloc(&base_, total), err, "cudaMalloc")) {
@@ -150,7 +168,14 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   }
   d_ctl_ = reinterpret_cast<TileCtl*>(base_ + off_ctl);
   d_desc_ = reinterpret_cast<TileDesc*>(base_ + off_desc);
+  d_first_ = reinterpret_cast<uint64_t*>(base_ + off_first);
   d_work_ = reinterpret_cast<WorkCtl*>(base_ + off_work);
+  if (!check(cudaMemcpyAsync(d_first_, first_.data(), nt * sizeof(uint64_t),
+                             cudaMemcpyHostToDevice, stream_),
+             err, "upload of the cell offsets")) {
+    destroy();
+    return false;
+  }
   host_.resize(nt);
   for (size_t i = 0; i < nt; ++i) {
     const TileSpec& t = tiles[i];
@@ -480,6 +505,130 @@ bool TileSet::read_partials(uint32_t tile, Partial* out, std::string* err) {
              err, "read-back of the records"))
     return false;
   return wait(err);
+}
+
+bool TileSet::write_all(const double* h, const double* hu, const double* hv, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = total_cells_;
+  if (!ensure_staging(3 * n * sizeof(double), err)) return false;
+  double* d = static_cast<double*>(staging_);
+  if (!check(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of the depth") ||
+      !check(cudaMemcpyAsync(d + n, hu, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of the momentum") ||
+      !check(cudaMemcpyAsync(d + 2 * n, hv, n * sizeof(double), cudaMemcpyHostToDevice, stream_),
+             err, "upload of the momentum") ||
+      !check(launch_scatter_state(d_desc_, tile_count(), d_first_, n, d, d + n, d + 2 * n, stream_),
+             err, "the states' conversion") ||
+      !check(enqueue_prime(stream_), err, "the prime pass"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::set_plane_all(int which, const double* v, double datum, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = total_cells_;
+  if (!ensure_staging(n * sizeof(double), err)) return false;
+  double* d = static_cast<double*>(staging_);
+  if (!check(cudaMemcpyAsync(d, v, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of an input") ||
+      !check(launch_scatter_plane(d_desc_, tile_count(), d_first_, n, d, datum, which, stream_),
+             err, "an input's conversion"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::set_flags_all(uint32_t flags_set, uint32_t flags_clear, uint32_t source_every,
+                            bool reset_phase, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  for (TileDesc& d : host_) {
+    d.flags = (d.flags & ~flags_clear) | flags_set;
+    d.source_every = source_every;
+  }
+  if (reset_phase) {
+    std::vector<TileCtl> ctl(tile_count());
+    if (!check(cudaMemcpyAsync(ctl.data(), d_ctl_, ctl.size() * sizeof(TileCtl),
+                               cudaMemcpyDeviceToHost, stream_),
+               err, "read-back of the control blocks") ||
+        !wait(err))
+      return false;
+    for (TileCtl& c : ctl) c.src_phase = 0u;
+    if (!check(cudaMemcpyAsync(d_ctl_, ctl.data(), ctl.size() * sizeof(TileCtl),
+                               cudaMemcpyHostToDevice, stream_),
+               err, "upload of the control blocks"))
+      return false;
+  }
+  if (!check(cudaMemcpyAsync(d_desc_, host_.data(), host_.size() * sizeof(TileDesc),
+                             cudaMemcpyHostToDevice, stream_),
+             err, "upload of the tiles"))
+    return false;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
+  const int occ = tick_occupancy(shape_, fixed_, any_manning());
+  grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
+  return wait(err);
+}
+
+bool TileSet::read_all_bits(float* out, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const size_t n = total_cells_;
+  if (!ensure_staging(kStatePlanes * n * sizeof(float), err)) return false;
+  float* d = static_cast<float*>(staging_);
+  if (!check(launch_gather_state(d_desc_, tile_count(), d_first_, n, d, stream_), err,
+             "the states' gather") ||
+      !check(cudaMemcpyAsync(out, d, kStatePlanes * n * sizeof(float), cudaMemcpyDeviceToHost,
+                             stream_),
+             err, "read-back of the states"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::flush_all(std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(launch_flush_all(fixed_, d_desc_, tile_count(), stream_), err, "the flush")) return false;
+  return wait(err);
+}
+
+bool TileSet::read_all_ctl(TileCtl* out, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(cudaMemcpyAsync(out, d_ctl_, tile_count() * sizeof(TileCtl), cudaMemcpyDeviceToHost,
+                             stream_),
+             err, "read-back of the ledgers"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::snapshot(std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (snap_ == nullptr && !check(cudaMalloc(&snap_, mutable_bytes_), err, "cudaMalloc")) {
+    snap_ = nullptr;
+    return false;
+  }
+  if (!check(cudaMemcpyAsync(snap_, base_, mutable_bytes_, cudaMemcpyDeviceToDevice, stream_), err,
+             "the snapshot"))
+    return false;
+  return wait(err);
+}
+
+bool TileSet::restore(std::string* err) {
+  if (snap_ == nullptr) {
+    if (err) *err = "water_live: no snapshot";
+    return false;
+  }
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  if (!check(cudaMemcpyAsync(base_, snap_, mutable_bytes_, cudaMemcpyDeviceToDevice, stream_), err,
+             "the restore"))
+    return false;
+  return wait(err);
+}
+
+void TileSet::drop_snapshot() {
+  if (snap_ != nullptr) {
+    cudaSetDevice(device_);
+    cudaStreamSynchronize(stream_);
+    cudaFree(snap_);
+    snap_ = nullptr;
+  }
 }
 
 }  // namespace wlc

@@ -60,6 +60,23 @@ class TileSet {
   bool length_pass(uint32_t tile, float max_dt, std::string* err);
   bool wait(std::string* err);
 
+  // ---- whole batches: arrays of every tile's cells, tile after tile in index order ---------
+  bool write_all(const double* h, const double* hu, const double* hv, std::string* err);
+  bool set_plane_all(int which, const double* v, double datum, std::string* err);
+  bool set_flags_all(uint32_t flags_set, uint32_t flags_clear, uint32_t source_every,
+                     bool reset_phase, std::string* err);
+  // Every tile's current copy (four planes a tile, 4 * first_cell(t) floats before tile t).
+  bool read_all_bits(float* out, std::string* err);
+  bool flush_all(std::string* err);
+  bool read_all_ctl(TileCtl* out, std::string* err);
+  uint64_t first_cell(uint32_t tile) const { return first_[tile]; }
+  // A copy of everything a tick changes (states, records, control blocks), and its restoration:
+  // the autotuner's trial ticks leave the simulation where it was.
+  bool snapshot(std::string* err);
+  bool restore(std::string* err);
+  void drop_snapshot();
+  const std::vector<uint32_t>& order() const { return order_; }
+
   uint32_t tile_count() const { return uint32_t(host_.size()); }
   const TileDesc& desc(uint32_t tile) const { return host_[tile]; }
   uint64_t cells(uint32_t tile) const { return uint64_t(host_[tile].nx) * host_[tile].ny; }
@@ -94,6 +111,10 @@ class TileSet {
   uint32_t n_items_ = 0;
   int grid_ = 0;
   uint64_t total_cells_ = 0;
+  std::vector<uint64_t> first_;  // each tile's first cell in the concatenated arrays
+  uint64_t* d_first_ = nullptr;
+  size_t mutable_bytes_ = 0;     // the leading part of the allocation a tick writes
+  void* snap_ = nullptr;
   void* staging_ = nullptr;  // device staging for uploads and read-backs
   size_t staging_bytes_ = 0;
   std::vector<uint32_t> order_;

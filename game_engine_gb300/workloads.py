@@ -43,7 +43,20 @@ def _lattice(ix, iy, salt):
 
 
 def fbm(nx: int, ny: int, height: float, seed: int, octaves: int = 6) -> np.ndarray:
-    """nx * ny heights in [0, height] (row-major, cell (x, y) at y * nx + x)."""
+    """nx * ny heights in [0, height] (row-major, cell (x, y) at y * nx + x), by the library's
+    threaded generator (wl_util_fbm), which gives the same doubles as fbm_numpy."""
+    import ctypes as C
+    from . import lib
+    out = np.empty(nx * ny)
+    rc = lib().wl_util_fbm(out.ctypes.data_as(C.POINTER(C.c_double)), nx, ny, float(height),
+                           int(seed) & 0xFFFFFFFFFFFFFFFF, octaves)
+    if rc != 0:
+        raise ValueError("wl_util_fbm refused its arguments")
+    return out
+
+
+def fbm_numpy(nx: int, ny: int, height: float, seed: int, octaves: int = 6) -> np.ndarray:
+    """The same fBm in numpy (the generator's statement; a test holds the two equal)."""
     side = max(nx, ny)
     base = max(side / 4.0, 1.0)
     ys, xs = np.meshgrid(np.arange(ny, dtype=np.float64), np.arange(nx, dtype=np.float64),

@@ -177,6 +177,78 @@ int wl_write_state_device(wl_step* step, const float* planes, wl_stream stream);
  * until the next call on the handle. */
 int wl_device_planes(wl_step* step, float** planes, float** bed, char* err, size_t err_len);
 
+/* ---- the batched form: many tiles, one persistent launch per tick -------------------------- *
+ * No counterpart call in the reference, which steps one rectangle per DeviceStep; each tile here
+ * is stepped exactly as a DeviceStep of its size would step it (the same bytes), and the reference's
+ * designed-but-unbuilt tile system (docs/subsystems/water_live.md:74-90) is what it serves.
+ * Arrays passed for the whole batch hold every tile's nx * ny cells, tile after tile in index
+ * order; wl_batch_tile_first gives a tile's first cell. */
+
+typedef struct wl_batch wl_batch;
+
+/* One tile: its size and its edges (water_state::Edges, water_state.h:62-67). */
+typedef struct wl_tile {
+  uint32_t nx, ny;
+  uint8_t west_open, east_open, south_open, north_open;
+} wl_tile;
+
+/* The launch's shape: rows of a 32-column work item (16, 32 or 64), the order items are dealt
+ * (0 tiles by index, 1 the largest tiles first), and the trial's time a tick. */
+typedef struct wl_tuning {
+  uint32_t block_rows;
+  uint32_t order;
+  float us_per_tick;
+} wl_tuning;
+
+/* `common` gives cell_m, gravity, cfl, dry_depth_m and device (its nx, ny and edges are unused). */
+int wl_batch_create(const wl_config* common, const wl_options* options, const wl_tile* tiles,
+                    uint32_t count, wl_batch** out, char* err, size_t err_len);
+void wl_batch_destroy(wl_batch* batch);
+uint32_t wl_batch_tile_count(const wl_batch* batch);
+uint64_t wl_batch_cell_count(const wl_batch* batch);
+uint64_t wl_batch_tile_first(const wl_batch* batch, uint32_t tile);
+
+/* write_state / set_bed / set_manning / set_source of every tile at once (total = all cells). */
+int wl_batch_write_state(wl_batch* batch, const double* depth, const double* momentum_x,
+                         const double* momentum_y, size_t total, char* err, size_t err_len);
+int wl_batch_set_bed(wl_batch* batch, const double* bed_m, size_t total, double datum_m, char* err,
+                     size_t err_len);
+int wl_batch_set_manning(wl_batch* batch, const double* manning, size_t total, char* err,
+                         size_t err_len);
+int wl_batch_set_source(wl_batch* batch, const double* source_m_per_s, size_t total,
+                        uint32_t every, int compensate, char* err, size_t err_len);
+
+/* `count` ticks of every tile, one persistent launch each, enqueued without waiting. */
+int wl_batch_enqueue_ticks(wl_batch* batch, wl_stream stream, uint32_t count, float max_dt);
+/* The same on the batch's own stream, replayed from a captured CUDA graph when use_graph, and
+ * waited for. */
+int wl_batch_run_ticks(wl_batch* batch, uint32_t count, float max_dt, int use_graph, char* err,
+                       size_t err_len);
+/* The per-tile-launch form, for comparison: one launch per tile per tick. */
+int wl_batch_enqueue_tile_tick(wl_batch* batch, wl_stream stream, uint32_t tile, float max_dt);
+int wl_batch_run_tile_ticks(wl_batch* batch, uint32_t count, float max_dt, int use_graph,
+                            char* err, size_t err_len);
+
+/* Read-backs: one tile's four planes (4 * nx * ny floats), every tile's (tile after tile), each
+ * tile's FNV-1a state hash, each tile's ledger (after a flush, as read_ledger does). */
+int wl_batch_read_tile_bits(wl_batch* batch, uint32_t tile, float* planes, size_t count, char* err,
+                            size_t err_len);
+int wl_batch_read_all_bits(wl_batch* batch, float* planes, size_t count, char* err, size_t err_len);
+uint64_t wl_batch_tile_hash(wl_batch* batch, uint32_t tile, char* err, size_t err_len);
+int wl_batch_tile_hashes(wl_batch* batch, uint64_t* out, uint32_t count, char* err,
+                         size_t err_len);
+int wl_batch_read_ledgers(wl_batch* batch, wl_ledger* out, uint32_t count, char* err,
+                          size_t err_len);
+
+/* The autotuner: times every block shape and item order on the batch itself for `trial_ticks`
+ * ticks (the trials are undone), keeps the fastest, and caches it per (SM count, tile-size
+ * histogram) for the process (and across processes in the file WLCUDA_TUNING_CACHE names). */
+int wl_batch_autotune(wl_batch* batch, float max_dt, uint32_t trial_ticks, wl_tuning* chosen,
+                      char* err, size_t err_len);
+int wl_batch_set_tuning(wl_batch* batch, const wl_tuning* tuning, char* err, size_t err_len);
+int wl_batch_get_tuning(const wl_batch* batch, wl_tuning* out);
+wl_stream wl_batch_stream(wl_batch* batch);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
