@@ -303,6 +303,66 @@ def run_plain(args, tile, rank, world):
     return out
 
 
+def run_tiles(steps: int, warmup: int, count: int = 4096, ticks: int = 200):
+    """The batched configuration: `count` tiles of seeded uneven sides, `ticks` ticks a step, one
+    persistent CUDA-graph-captured launch a tick after the autotuner's choice; beside it the
+    per-tile-launch form (one launch per tile per tick) on the same tiles, its best of three
+    launch strategies."""
+    import torch
+    from game_engine_gb300 import workloads
+    from game_engine_gb300.batch import Batch, concat
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    tiles = workloads.tiles_4096(count)
+    sides = [(t.nx, t.ny) for t in tiles]
+    b = Batch(sides, device=dev)
+    b.set_bed(concat(tiles, "bed"))
+    h0 = concat(tiles, "h")
+    b.write_state(h0)
+    cells = b.cells
+    del tiles
+    tuning = b.autotune(workloads.MAX_DT, trial_ticks=4)
+    stream = torch.cuda.ExternalStream(b.stream())
+    for _ in range(warmup):
+        b.run_ticks(ticks // 4, workloads.MAX_DT)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms = 0.0
+    for _ in range(steps):
+        b.write_state(h0)  # the same initial state every step (untimed)
+        ev[0].record(stream)
+        b.run_ticks(ticks, workloads.MAX_DT, graph=True)
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        ms += ev[0].elapsed_time(ev[1])
+    batched = cells * ticks * steps / (ms * 1e-3)
+    # The per-tile-launch form on the same tiles, given its best shape (16-row items, the most
+    # parallel) and timed three ways: one stream, one stream from a captured graph, and tiles
+    # dealt to 64 concurrent streams as independent steps would run. Fewer ticks: it is slow.
+    per_ticks = 10
+    b.set_tuning(16, 0)
+    per = {}
+    for name, graph, nstreams in (("stream", False, 1), ("graph", True, 1), ("streams_64", False, 64)):
+        b.write_state(h0)
+        b.run_tile_ticks(2, workloads.MAX_DT, graph=graph, streams=nstreams)
+        ev[0].record(stream)
+        b.run_tile_ticks(per_ticks, workloads.MAX_DT, graph=graph, streams=nstreams)
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        per[name] = cells * per_ticks / (ev[0].elapsed_time(ev[1]) * 1e-3)
+    per_tile = max(per.values())
+    b.close()
+    return {
+        "workload": f"{count} tiles, sides from {workloads.TILE_SIDES}, own fBm 0-20 m and a 2 m "
+                    f"column each, {ticks} ticks a step, max_dt 0.01 s",
+        "cells": cells, "tiles": count, "value": batched, "unit": "cell-updates/s",
+        "ms_per_tick": ms / (steps * ticks), "tuning": tuning,
+        "per_tile_launch": {"value": per_tile, "unit": "cell-updates/s", "forms": per,
+                            "block_rows": 16},
+        "speedup_vs_per_tile_launch": batched / per_tile,
+        "launches_per_tick": {"batched": 1, "per_tile": count},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,6 +371,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain_2048")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched and adjoint measurements beside the headline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -318,6 +380,11 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from game_engine_gb300 import workloads
 
+    if args.workload == "tiles_4096":
+        if rank == 0:
+            out = run_tiles(args.steps, args.warmup)
+            print(json.dumps(out), flush=True)
+        return
     if args.workload == "plain_2048":
         tile = workloads.plain_2048()
     elif args.workload == "plain_256":
@@ -335,6 +402,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if os.environ.get("WL_BENCH_NCCL") else "gloo")
     out = run_plain(args, tile, rank, world)
+    if rank == 0 and not args.no_extras:
+        out["batched"] = run_tiles(max(1, min(args.steps, 3)), 1)
     if rank == 0:
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(tile, os.cpu_count() or 1)

@@ -106,7 +106,8 @@ SIGNATURES = {
     "wl_batch_enqueue_ticks": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32, C.c_float]),
     "wl_batch_run_ticks": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_int, *_err]),
     "wl_batch_enqueue_tile_tick": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32, C.c_float]),
-    "wl_batch_run_tile_ticks": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_int, *_err]),
+    "wl_batch_run_tile_ticks": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_int,
+                                          C.c_uint32, *_err]),
     "wl_batch_read_tile_bits": (C.c_int, [C.c_void_p, C.c_uint32, _fp, C.c_size_t, *_err]),
     "wl_batch_read_all_bits": (C.c_int, [C.c_void_p, _fp, C.c_size_t, *_err]),
     "wl_batch_tile_hash": (C.c_uint64, [C.c_void_p, C.c_uint32, *_err]),

@@ -114,9 +114,9 @@ class Batch:
     def enqueue_ticks(self, stream, count, max_dt):
         self._check(lib().wl_batch_enqueue_ticks(self._h, stream, int(count), float(max_dt)))
 
-    def run_tile_ticks(self, count, max_dt, graph=True):
+    def run_tile_ticks(self, count, max_dt, graph=True, streams=1):
         self._check(lib().wl_batch_run_tile_ticks(self._h, int(count), float(max_dt), int(graph),
-                                                  self._buf, len(self._buf)))
+                                                  int(streams), self._buf, len(self._buf)))
 
     def read_tile_bits(self, k):
         nx, ny = self.sides[k]

@@ -39,9 +39,11 @@ struct wl_batch {
   cudaGraphExec_t tile_graph = nullptr;
   float tile_graph_max_dt = 0.0f;
   uint64_t tile_graph_key = 0;
+  std::vector<cudaStream_t> side_streams;  // the per-tile form's concurrent streams
   ~wl_batch() {
     if (graph != nullptr) cudaGraphExecDestroy(graph);
     if (tile_graph != nullptr) cudaGraphExecDestroy(tile_graph);
+    for (cudaStream_t s : side_streams) cudaStreamDestroy(s);
   }
 };
 
@@ -331,14 +333,41 @@ int wl_batch_enqueue_tile_tick(wl_batch* b, wl_stream stream, uint32_t tile, flo
   return b->set.enqueue_tile_tick(st, tile, max_dt) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
 }
 
-int wl_batch_run_tile_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph, char* err,
-                            size_t err_len) {
+int wl_batch_run_tile_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph,
+                            uint32_t streams, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
   if (cudaSetDevice(b->set.device()) != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
   cudaStream_t st = b->set.stream();
   const uint32_t n = b->set.tile_count();
-  if (use_graph) {
+  if (streams > 1) {
+    // Tiles dealt round-robin to concurrent streams, as independent steps with their own streams
+    // would run; a tile's ticks stay in order on its stream.
+    while (b->side_streams.size() < streams) {
+      cudaStream_t s = nullptr;
+      if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaStreamCreate");
+      b->side_streams.push_back(s);
+    }
+    cudaEvent_t start;
+    cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    cudaEventRecord(start, st);
+    for (uint32_t k = 0; k < streams; ++k) cudaStreamWaitEvent(b->side_streams[k], start, 0);
+    for (uint32_t k = 0; k < count; ++k)
+      for (uint32_t t = 0; t < n; ++t)
+        if (b->set.enqueue_tile_tick(b->side_streams[t % streams], t, max_dt) != cudaSuccess) {
+          cudaEventDestroy(start);
+          return fail(err, err_len, WL_ERR_CUDA, "water_live: a tile's tick");
+        }
+    for (uint32_t k = 0; k < streams; ++k) {
+      cudaEvent_t done;
+      cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+      cudaEventRecord(done, b->side_streams[k]);
+      cudaStreamWaitEvent(st, done, 0);
+      cudaEventDestroy(done);
+    }
+    cudaEventDestroy(start);
+  } else if (use_graph) {
     const uint64_t key = launch_key(b);
     if (b->tile_graph == nullptr || b->tile_graph_max_dt != max_dt || b->tile_graph_key != key) {
       if (b->tile_graph != nullptr) cudaGraphExecDestroy(b->tile_graph);

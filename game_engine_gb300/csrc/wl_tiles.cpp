@@ -154,8 +154,10 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   total += align_up(nt * sizeof(TileDesc));
   const size_t off_first = total;
   total += align_up(nt * sizeof(uint64_t));
+  // The work counters: one for launches over the whole set, one per tile for its own launches
+  // (tiles launched alone may run concurrently on different streams).
   const size_t off_work = total;
-  total += align_up(sizeof(WorkCtl));
+  total += align_up((1 + nt) * sizeof(WorkCtl));
   if (!check(cudaMalloc(&base_, total), err, "cudaMalloc")) {
     base_ = nullptr;
     destroy();
@@ -330,7 +332,7 @@ cudaError_t TileSet::enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_
   TickArgs a;
   a.tiles = d_desc_ + tile;
   a.item_tile = nullptr;
-  a.work = d_work_;
+  a.work = d_work_ + 1 + tile;
   a.n_items = host_[tile].items;
   a.max_dt = max_dt;
   int sms = 0;

@@ -224,10 +224,12 @@ int wl_batch_enqueue_ticks(wl_batch* batch, wl_stream stream, uint32_t count, fl
  * waited for. */
 int wl_batch_run_ticks(wl_batch* batch, uint32_t count, float max_dt, int use_graph, char* err,
                        size_t err_len);
-/* The per-tile-launch form, for comparison: one launch per tile per tick. */
+/* The per-tile-launch form, for comparison: one launch per tile per tick, on the batch's stream
+ * (captured in a graph when use_graph) or, when streams > 1, dealt round-robin to that many
+ * concurrent streams as independent steps would be. */
 int wl_batch_enqueue_tile_tick(wl_batch* batch, wl_stream stream, uint32_t tile, float max_dt);
 int wl_batch_run_tile_ticks(wl_batch* batch, uint32_t count, float max_dt, int use_graph,
-                            char* err, size_t err_len);
+                            uint32_t streams, char* err, size_t err_len);
 
 /* Read-backs: one tile's four planes (4 * nx * ny floats), every tile's (tile after tile), each
  * tile's FNV-1a state hash, each tile's ledger (after a flush, as read_ledger does). */

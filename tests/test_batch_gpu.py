@@ -69,7 +69,8 @@ def test_per_tile_launches_give_the_same_bytes(gpu):
     load(c, tiles)
     a.run_ticks(25, 0.02, graph=True)
     c.run_tile_ticks(20, 0.02, graph=True)
-    c.run_tile_ticks(5, 0.02, graph=False)
+    c.run_tile_ticks(3, 0.02, graph=False)
+    c.run_tile_ticks(2, 0.02, graph=False, streams=3)
     assert np.array_equal(a.tile_hashes(), c.tile_hashes())
 
 
