@@ -2,7 +2,7 @@
 """Benchmark of the live-water tick on a GB300 (one JSON line on stdout).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload plain_2048|plain_256|tiles_4096]
+                    [--workload plain_2048|plain_256|tiles_4096|adjoint_512|tiles_256_adjoint]
 
 The metric is water cell-updates per second. A bench step is one pass of the workload over its
 configuration: for the default (plain_2048, the throughput configuration) 500 ticks of one
@@ -10,6 +10,11 @@ configuration: for the default (plain_2048, the throughput configuration) 500 ti
 (each step restores the initial state from a device copy, untimed work between steps flushes L2);
 `e2e` runs the same steps through the C ABI with host buffers: upload of the state, bed and source,
 the ticks, and the read-back of the state, every step.
+
+Beside the headline (unless --no-extras): `batched`, the 4096-tile configuration in one persistent
+graph-captured launch a tick against the per-tile-launch form; `adjoint` and `batched_adjoint`, the
+checkpointed sweep's seconds per tick (forward and reverse) against the plain tick's on the same
+tiles.
 
 `--impl reference` times the reference's CPU tick (the FP64 solver, water_state::Solver::step,
 restated in oracle/ and checked byte for byte against the reference's own build) on this host's
@@ -303,7 +308,7 @@ def run_plain(args, tile, rank, world):
     return out
 
 
-def run_tiles(steps: int, warmup: int, count: int = 4096, ticks: int = 200):
+def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
     """The batched configuration: `count` tiles of seeded uneven sides, `ticks` ticks a step, one
     persistent CUDA-graph-captured launch a tick after the autotuner's choice; beside it the
     per-tile-launch form (one launch per tile per tick) on the same tiles, its best of three
@@ -313,6 +318,7 @@ def run_tiles(steps: int, warmup: int, count: int = 4096, ticks: int = 200):
     from game_engine_gb300.batch import Batch, concat
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ticks = ticks or 200
     tiles = workloads.tiles_4096(count)
     sides = [(t.nx, t.ny) for t in tiles]
     b = Batch(sides, device=dev)
@@ -363,6 +369,142 @@ def run_tiles(steps: int, warmup: int, count: int = 4096, ticks: int = 200):
     }
 
 
+def _time_on(stream, fn, steps):
+    """Milliseconds of `steps` calls of fn, CUDA events on `stream` around each."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for a, b in ev:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def run_adjoint(steps: int, warmup: int, ticks: int = 0):
+    """The adjoint configuration (512 x 512, 2000 ticks, a checkpoint every 50, 64 probes): the
+    whole sweep (checkpoint pass, loss, recompute and reverse ticks) from one captured graph, in
+    seconds per tick, against the plain tick's own seconds per tick on the same tile."""
+    import torch
+    from game_engine_gb300 import lib, water_live as wl, workloads
+    from game_engine_gb300.adjoint import Adjoint
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    t = workloads.adjoint_512()
+    ticks, every, dt = ticks or t.meta["ticks"], t.meta["every"], t.meta["max_dt"]
+    probes = t.meta["probes"]
+
+    def make(bed):
+        s = wl.DeviceStep()
+        assert s.create(wl.Config(t.nx, t.ny, t.cell_m, device=dev)), s.error
+        assert s.set_bed(bed) and s.set_source(t.source) and s.write_state(t.h, t.hu, t.hv)
+        return s
+
+    # The targets: the plain tick on the bed plus N(0, 0.1 m).
+    tgt = make(workloads.perturbed_bed(t.bed, workloads.SEEDS["adjoint_512"]))
+    assert tgt.run_steps(ticks, dt), tgt.error
+    targets = tgt.read_state()[0][probes]
+    tgt.destroy()
+    step = make(t.bed)
+    a = Adjoint(step, ticks, every, probes, targets)
+    s_ptr = step.stream()
+    stream = torch.cuda.ExternalStream(s_ptr)
+    for _ in range(warmup):
+        a.run(dt)
+    sweep_ms = _time_on(stream, lambda: a.run(dt), steps)
+    loss, g_bed, g_src, limited = a.read()
+    launches = a.launches()
+    nbytes = a.device_bytes()
+    a.close()
+    # The plain tick's cost on the same tile: the same ticks from the same state.
+    init = torch.from_numpy(step.read_state_bits()).to(f"cuda:{dev}")
+    L = lib()
+
+    def forward():
+        assert L.wl_write_state_device(step.handle, C.c_void_p(init.data_ptr()), s_ptr) == 0
+        assert step.record(s_ptr, ticks, dt), step.error
+
+    for _ in range(warmup):
+        forward()
+    fwd_ms = _time_on(stream, forward, steps)
+    step.destroy()
+    sweep_tick = statistics.median(sweep_ms) * 1e-3 / ticks
+    fwd_tick = statistics.median(fwd_ms) * 1e-3 / ticks
+    return {
+        "workload": f"adjoint_512: {t.nx} x {t.ny}, {ticks} ticks of {dt} s, a checkpoint every "
+                    f"{every}, {len(probes)} probes, the source on at zero inflow, targets from a "
+                    f"run on the bed + N(0, 0.1 m)",
+        "metric": "fwd+adjoint s/tick", "value": sweep_tick, "unit": "s/tick",
+        "forward_s_per_tick": fwd_tick, "ratio_to_forward": sweep_tick / fwd_tick,
+        "loss": float(loss[0]), "shortened_ticks": int(limited[0]),
+        "gpu_launches_per_sweep": launches, "device_bytes": nbytes,
+        "grad_norms": {"bed": float(np.abs(g_bed).max()), "source": float(np.abs(g_src).max())},
+    }
+
+
+def run_tiles_adjoint(steps: int, warmup: int, ticks: int = 0, count: int = 256):
+    """The batched adjoint configuration (256 tiles, 500 ticks, a checkpoint every 25, 64 probes
+    a tile): the sweep over every tile in one launch a tick forward and reverse, from one captured
+    graph, against the batched plain tick on the same tiles."""
+    import torch
+    from game_engine_gb300 import workloads
+    from game_engine_gb300.adjoint import Adjoint
+    from game_engine_gb300.batch import Batch, concat
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    tiles = workloads.tiles_256_adjoint(count)
+    ticks, every, dt = (ticks or workloads.TILES_ADJOINT_TICKS, workloads.TILES_ADJOINT_EVERY,
+                        workloads.MAX_DT)
+    sides = [(t.nx, t.ny) for t in tiles]
+    seed = workloads.SEEDS["tiles_256_adjoint"]
+
+    def make(beds):
+        b = Batch(sides, device=dev)
+        b.set_bed(np.concatenate(beds))
+        b.set_source(concat(tiles, "source"))
+        b.write_state(concat(tiles, "h"))
+        return b
+
+    tgt = make([workloads.perturbed_bed(t.bed, seed + k) for k, t in enumerate(tiles)])
+    tgt.run_ticks(ticks, dt)
+    targets = [tgt.read_tile_bits(k)[:t.cells][t.meta["probes"]].astype(np.float64)
+               for k, t in enumerate(tiles)]
+    tgt.close()
+    b = make([t.bed for t in tiles])
+    b.autotune(dt, trial_ticks=3)
+    a = Adjoint(b, ticks, every, [t.meta["probes"] for t in tiles], targets)
+    stream = torch.cuda.ExternalStream(b.stream())
+    for _ in range(warmup):
+        a.run(dt)
+    sweep_ms = _time_on(stream, lambda: a.run(dt), steps)
+    loss, _, _, limited = a.read()
+    launches = a.launches()
+    nbytes = a.device_bytes()
+    a.close()
+    h0 = concat(tiles, "h")
+
+    def forward():
+        b.write_state(h0)
+        b.run_ticks(ticks, dt, graph=True)
+
+    forward()
+    fwd_ms = _time_on(stream, lambda: b.run_ticks(ticks, dt, graph=True), steps)
+    cells = b.cells
+    b.close()
+    sweep_tick = statistics.median(sweep_ms) * 1e-3 / ticks
+    fwd_tick = statistics.median(fwd_ms) * 1e-3 / ticks
+    return {
+        "workload": f"tiles_256_adjoint: {count} tiles, sides from "
+                    f"{workloads.ADJOINT_TILE_SIDES}, {cells} cells, {ticks} ticks of {dt} s, "
+                    f"a checkpoint every {every}, 64 probes a tile",
+        "metric": "fwd+adjoint s/tick", "value": sweep_tick, "unit": "s/tick",
+        "forward_s_per_tick": fwd_tick, "ratio_to_forward": sweep_tick / fwd_tick,
+        "loss_sum": float(loss.sum()), "shortened_ticks": int(limited.sum()),
+        "gpu_launches_per_sweep": launches, "device_bytes": nbytes,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -373,6 +515,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched and adjoint measurements beside the headline")
+    ap.add_argument("--ticks", type=int, default=0,
+                    help="ticks a step instead of the workload's (a short run for a profiler; "
+                         "the configuration's number is measured with the default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -380,9 +525,11 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from game_engine_gb300 import workloads
 
-    if args.workload == "tiles_4096":
+    if args.workload in ("tiles_4096", "adjoint_512", "tiles_256_adjoint"):
         if rank == 0:
-            out = run_tiles(args.steps, args.warmup)
+            fn = {"tiles_4096": run_tiles, "adjoint_512": run_adjoint,
+                  "tiles_256_adjoint": run_tiles_adjoint}[args.workload]
+            out = fn(args.steps, args.warmup, args.ticks)
             print(json.dumps(out), flush=True)
         return
     if args.workload == "plain_2048":
@@ -391,6 +538,8 @@ def main():
         tile = workloads.plain_256()
     else:
         raise SystemExit(f"unknown workload {args.workload}")
+    if args.ticks > 0:
+        tile.meta["ticks"] = args.ticks
 
     if args.impl == "reference":
         out = run_reference(args, tile, rank, world)
@@ -404,6 +553,8 @@ def main():
     out = run_plain(args, tile, rank, world)
     if rank == 0 and not args.no_extras:
         out["batched"] = run_tiles(max(1, min(args.steps, 3)), 1)
+        out["adjoint"] = run_adjoint(max(1, min(args.steps, 3)), 1)
+        out["batched_adjoint"] = run_tiles_adjoint(max(1, min(args.steps, 3)), 1)
     if rank == 0:
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(tile, os.cpu_count() or 1)

@@ -67,6 +67,7 @@ class Tuning(C.Structure):
 
 
 _u64p = C.POINTER(C.c_uint64)
+_u32p = C.POINTER(C.c_uint32)
 
 # name -> (restype, argtypes); every symbol include/wlcuda.h declares.
 SIGNATURES = {
@@ -118,6 +119,18 @@ SIGNATURES = {
     "wl_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "wl_batch_stream": (wl_stream, [C.c_void_p]),
     "wl_util_fbm": (C.c_int, [_dp, C.c_uint32, C.c_uint32, C.c_double, C.c_uint64, C.c_uint32]),
+    # the adjoint
+    "wl_adjoint_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _u32p, _dp,
+                                    C.POINTER(C.c_void_p), *_err]),
+    "wl_batch_adjoint_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, _u32p, _u32p, _dp,
+                                          C.POINTER(C.c_void_p), *_err]),
+    "wl_adjoint_destroy": (None, [C.c_void_p]),
+    "wl_adjoint_enqueue": (C.c_int, [C.c_void_p, C.c_float]),
+    "wl_adjoint_run": (C.c_int, [C.c_void_p, C.c_float, C.c_int, *_err]),
+    "wl_adjoint_read": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _u32p, *_err]),
+    "wl_adjoint_read_final": (C.c_int, [C.c_void_p, _fp, *_err]),
+    "wl_adjoint_launches": (C.c_uint32, [C.c_void_p]),
+    "wl_adjoint_device_bytes": (C.c_uint64, [C.c_void_p]),
 }
 
 

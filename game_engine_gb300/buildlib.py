@@ -1,8 +1,10 @@
 """Builds libwlcuda.so (the CUDA kernels and the C ABI) in-tree for sm_103a with nvcc.
 
-No contraction and IEEE division and square root in every translation unit: the step's bytes must
-equal the CPU restatement's. The translation units compile in parallel; the result lands in
-``game_engine_gb300/lib/libwlcuda.so`` (objects in ``game_engine_gb300/_build``).
+No contraction and IEEE division and square root in every translation unit of the tick: the step's
+bytes must equal the CPU restatement's. The adjoint's unit takes contraction for its reverse march
+only (its forward march is spelled in correctly rounded intrinsics throughout). The translation
+units compile in parallel; the result lands in ``game_engine_gb300/lib/libwlcuda.so`` (objects in
+``game_engine_gb300/_build``).
 """
 from __future__ import annotations
 
@@ -20,10 +22,15 @@ LIB = os.path.join(LIB_DIR, "libwlcuda.so")
 
 SOURCES = ["wl_kernels.cu", "wl_adjoint.cu", "wl_tiles.cpp", "wl_api.cpp", "wl_batch.cpp",
            "wl_util.cpp"]
-HEADERS = ["wl_device.cuh", "wl_kernels.h", "wl_tiles.h", "wl_adjoint.h", "wl_batch.h"]
+HEADERS = ["wl_device.cuh", "wl_kernels.h", "wl_tiles.h", "wl_adjoint.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NUMERICS = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
+# The adjoint's translation unit: its forward march spells every operation as a correctly rounded
+# intrinsic (no contraction can touch it) and its reverse march is a derivative held to a
+# tolerance, so contraction is on there.
+NUMERICS_BY_SOURCE = {"wl_adjoint.cu": ["--fmad=true", "-prec-div=true", "-prec-sqrt=true",
+                                        "-ftz=false"]}
 HOST = ["-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math,-Wall"]
 
 
@@ -56,7 +63,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(obj)
         if not force and not _stale(obj, [path] + headers):
             continue
-        cmd = [cc, "-std=c++17", "-O3", "-lineinfo", *ARCH, *NUMERICS, *HOST,
+        numerics = NUMERICS_BY_SOURCE.get(src, NUMERICS)
+        cmd = [cc, "-std=c++17", "-O3", "-lineinfo", *ARCH, *numerics, *HOST,
                "-I", os.path.join(ROOT, "include"), "-c", path, "-o", obj]
         if src.endswith(".cpp"):
             cmd[1:1] = ["-x", "cu"]

@@ -2,6 +2,7 @@
 // Each function names the reference call it stands in for (systems/water_live/src/water_live.cpp).
 #include "wlcuda.h"
 
+#include "wl_adjoint.h"
 #include "wl_tiles.h"
 
 #include <cstddef>
@@ -108,10 +109,21 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
   if (config->north_open) s->flags |= WL_FLAG_NORTH_OPEN;
   if (s->options.stored_faces) s->flags |= WL_FLAG_STORED_FACES;
   t.open_edges = s->flags & 15u;
-  // The block shape: 32 x 32 unless WLCUDA_BLOCK_ROWS names 16 or 64 (a tuning override).
+  // The block shape: 32 x 32, or the split 32 x 16 items where 32 x 32 items would leave the
+  // device short of warps (fewer than eight an SM); WLCUDA_BLOCK_ROWS (4, 16, 32 or 64) overrides.
   wlc::BlockShape shape = wlc::BlockShape::k32x32;
+  {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, config->device) !=
+        cudaSuccess)
+      sms = 0;
+    const uint64_t items32 = uint64_t((config->nx + 31u) / 32u) * ((config->ny + 31u) / 32u);
+    if (sms > 0 && items32 < uint64_t(sms) * 8u) shape = wlc::BlockShape::k32x16s;
+  }
   if (const char* rows = std::getenv("WLCUDA_BLOCK_ROWS")) {
+    if (std::strcmp(rows, "4") == 0) shape = wlc::BlockShape::k32x16s;
     if (std::strcmp(rows, "16") == 0) shape = wlc::BlockShape::k32x16;
+    if (std::strcmp(rows, "32") == 0) shape = wlc::BlockShape::k32x32;
     if (std::strcmp(rows, "64") == 0) shape = wlc::BlockShape::k32x64;
   }
   std::string msg;
@@ -358,6 +370,19 @@ int wl_device_planes(wl_step* s, float** planes, float** bed, char* err, size_t 
   if (planes) *planes = s->set.device_state(0, c.cur & 1u);
   if (bed) *bed = const_cast<float*>(s->set.desc(0).bed);
   return WL_OK;
+}
+
+int wl_adjoint_create(wl_step* step, uint32_t ticks, uint32_t every, uint32_t n_probes,
+                      const uint32_t* probes, const double* targets, wl_adjoint** out, char* err,
+                      size_t err_len) {
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no handle to fill");
+  *out = nullptr;
+  if (!valid(step)) return fail(err, err_len, WL_ERR_INVALID, "water_live: no step");
+  if (n_probes > 0 && (probes == nullptr || targets == nullptr))
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no probes or targets");
+  const uint32_t first[2] = {0u, n_probes};
+  return wl_adjoint_create_over(&step->set, ticks, every, first, probes, targets, out, err,
+                                err_len);
 }
 
 }  // extern "C"

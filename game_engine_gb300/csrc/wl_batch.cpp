@@ -3,6 +3,7 @@
 // the order work items are dealt in chosen by timing the candidates on the batch itself.
 #include "wlcuda.h"
 
+#include "wl_adjoint.h"
 #include "wl_tiles.h"
 
 #include <algorithm>
@@ -66,8 +67,12 @@ int cuda_fail(char* err, size_t len, const std::string& msg) {
 bool valid(const wl_batch* b) { return b != nullptr && b->set.valid(); }
 const char* k_no_device = "water_live: no device";
 
+// block_rows: the rows one warp marches (4: the 32 x 16 items split over a CTA's four warps).
 BlockShape shape_of_rows(uint32_t rows) {
-  return rows == 16 ? BlockShape::k32x16 : rows == 64 ? BlockShape::k32x64 : BlockShape::k32x32;
+  return rows == 4    ? BlockShape::k32x16s
+         : rows == 16 ? BlockShape::k32x16
+         : rows == 64 ? BlockShape::k32x64
+                      : BlockShape::k32x32;
 }
 
 // Work-item orders: 0 tiles by index, 1 the largest tiles first.
@@ -487,7 +492,8 @@ int wl_batch_read_ledgers(wl_batch* b, wl_ledger* out, uint32_t count, char* err
 
 int wl_batch_set_tuning(wl_batch* b, const wl_tuning* t, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
-  if (t == nullptr || (t->block_rows != 16 && t->block_rows != 32 && t->block_rows != 64) ||
+  if (t == nullptr ||
+      (t->block_rows != 4 && t->block_rows != 16 && t->block_rows != 32 && t->block_rows != 64) ||
       t->order > 1)
     return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: a tuning out of range");
   std::string msg;
@@ -520,7 +526,7 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
     // writes is taken first and put back after.
     if (!b->set.snapshot(&msg)) return cuda_fail(err, err_len, msg);
     best.us_per_tick = std::numeric_limits<float>::infinity();
-    for (uint32_t rows : {16u, 32u, 64u}) {
+    for (uint32_t rows : {4u, 16u, 32u, 64u}) {
       for (uint32_t order : {0u, 1u}) {
         if (!b->set.reshape(shape_of_rows(rows), item_order(b->specs, order), &msg) ||
             !b->set.restore(&msg))
@@ -550,6 +556,20 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
 
 wl_stream wl_batch_stream(wl_batch* b) {
   return valid(b) ? reinterpret_cast<wl_stream>(b->set.stream()) : nullptr;
+}
+
+int wl_batch_adjoint_create(wl_batch* batch, uint32_t ticks, uint32_t every,
+                            const uint32_t* probe_first, const uint32_t* probes,
+                            const double* targets, wl_adjoint** out, char* err, size_t err_len) {
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no handle to fill");
+  *out = nullptr;
+  if (!valid(batch)) return fail(err, err_len, WL_ERR_INVALID, "water_live: no batch");
+  if (probe_first == nullptr)
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no probe offsets");
+  if (probe_first[batch->set.tile_count()] > 0 && (probes == nullptr || targets == nullptr))
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no probes or targets");
+  return wl_adjoint_create_over(&batch->set, ticks, every, probe_first, probes, targets, out, err,
+                                err_len);
 }
 
 }  // extern "C"

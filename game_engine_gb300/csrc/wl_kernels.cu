@@ -298,9 +298,40 @@ __device__ __forceinline__ float4 shfl_down4(const float4& v) {
                      __shfl_down_sync(0xffffffffu, v.z, 1), __shfl_down_sync(0xffffffffu, v.w, 1));
 }
 
-// One item: a band of 32 columns by up to H rows of one tile, one tick.
-template <bool FIXED, bool MANNING, int H>
-__device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, uint32_t& ia,
+// The end of a split march: this warp's rows past the grid's edge hold nothing in the shared ring,
+// its largest speeds go to the item's two groups (s_ab: a, b of the west group, a, b of the east)
+// and the quantities some cell holds to s_need (1 open-edge, 2 roundoff).
+__device__ __forceinline__ void split_partials(float* ring, int ring_row0, int rows, uint32_t ga,
+                                               uint32_t gb, bool opn_seen, bool rnd_seen,
+                                               uint32_t* s_ab, uint32_t* s_need) {
+  const int lane = threadIdx.x & 31;
+  for (int r = max(rows, 0); r < 4; ++r) {
+    const int slot = (ring_row0 + r) * kStrip + lane;
+    ring[slot] = 0.0f;
+    ring[16 * kStrip + slot] = 0.0f;
+    ring[32 * kStrip + slot] = 0.0f;
+  }
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) {
+    ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
+    gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
+  }
+  const bool any_opn = __any_sync(0xffffffffu, opn_seen);
+  const bool any_rnd = __any_sync(0xffffffffu, rnd_seen);
+  if ((lane & 15) == 0) {
+    atomicMax(&s_ab[(lane >> 4) * 2], ga);
+    atomicMax(&s_ab[(lane >> 4) * 2 + 1], gb);
+  }
+  if (lane == 0 && (any_opn || any_rnd)) atomicOr(s_need, (any_opn ? 1u : 0u) | (any_rnd ? 2u : 0u));
+}
+
+// One item: a band of 32 columns by up to H rows of one tile, one tick. SPLIT: the warp's H rows
+// are rows ring_row0 .. ring_row0 + H - 1 of a 16-row item that the CTA's warps share; their
+// volumes go to the CTA's ring and the records are the CTA's (split_partials, then group_records
+// after the CTA's barrier).
+template <bool FIXED, bool MANNING, int H, bool SPLIT>
+__device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, float* ring,
+                      int ring_row0, uint32_t* s_ab, uint32_t* s_need, uint32_t& ia,
                       uint32_t& ib) {
   using O = Ops<FIXED>;
   const int lane = threadIdx.x & 31;
@@ -311,6 +342,10 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, u
   const bool col = gx < nx;
   const int last = min(kStrip - 1, nx - 1 - X0);  // the band's last live lane
   const int rows = min(H, ny - Y0);
+  if (SPLIT && rows <= 0) {  // a warp below the grid's last row
+    split_partials(ring, ring_row0, 0, 0u, 0u, false, false, s_ab, s_need);
+    return;
+  }
   const float* in = T.state[it.cur];
   float* out = T.state[it.cur ^ 1u];
   const float* ph = in;
@@ -342,11 +377,12 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, u
         ga = max(ga, __float_as_uint(ax));
         gb = max(gb, __float_as_uint(ay));
       }
-      if ((j & 15) == 15 || j == rows - 1) {
-        group_records(T, rec_out, X0, gy / 16, ga, gb, wm.ring, false, false, false, ia, ib);
+      if (!SPLIT && ((j & 15) == 15 || j == rows - 1)) {
+        group_records(T, rec_out, X0, gy / 16, ga, gb, ring, false, false, false, ia, ib);
         ga = gb = 0u;
       }
     }
+    if (SPLIT) split_partials(ring, ring_row0, rows, ga, gb, false, false, s_ab, s_need);
     return;
   }
 
@@ -523,23 +559,23 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, u
     }
     ga = max(ga, __float_as_uint(ax));
     gb = max(gb, __float_as_uint(ay));
-    const int slot = (j & 15) * kStrip + lane;
-    wm.ring[slot] = csrc;
-    wm.ring[16 * kStrip + slot] = copn;
-    wm.ring[32 * kStrip + slot] = crnd;
+    const int slot = ((ring_row0 + j) & 15) * kStrip + lane;
+    ring[slot] = csrc;
+    ring[16 * kStrip + slot] = copn;
+    ring[32 * kStrip + slot] = crnd;
     opn_seen |= copn != 0.0f;
     rnd_seen |= crnd != 0.0f;
-    if ((j & 15) == 15 || j == rows - 1) {
+    if (!SPLIT && ((j & 15) == 15 || j == rows - 1)) {
       // The group row ends: rows past the grid's edge hold nothing, then the records.
       for (int r = (j & 15) + 1; r < 16; ++r) {
-        wm.ring[r * kStrip + lane] = 0.0f;
-        wm.ring[(16 + r) * kStrip + lane] = 0.0f;
-        wm.ring[(32 + r) * kStrip + lane] = 0.0f;
+        ring[r * kStrip + lane] = 0.0f;
+        ring[(16 + r) * kStrip + lane] = 0.0f;
+        ring[(32 + r) * kStrip + lane] = 0.0f;
       }
       __syncwarp();
       const bool need_opn = __any_sync(0xffffffffu, opn_seen);
       const bool need_rnd = __any_sync(0xffffffffu, rnd_seen);
-      group_records(T, rec_out, X0, gy / 16, ga, gb, wm.ring, src_on, need_opn, need_rnd, ia, ib);
+      group_records(T, rec_out, X0, gy / 16, ga, gb, ring, src_on, need_opn, need_rnd, ia, ib);
       ga = gb = 0u;
       opn_seen = rnd_seen = false;
     }
@@ -551,6 +587,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, u
     fs = fn;
     i += nx;
   }
+  if (SPLIT) split_partials(ring, ring_row0, rows, ga, gb, opn_seen, rnd_seen, s_ab, s_need);
 }
 
 // The persistent tick: every work item of every tile, one tick.
@@ -592,7 +629,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
       __syncwarp();
     }
     uint32_t ia = 0u, ib = 0u;
-    march<FIXED, MANNING, H>(T, it, wm, ia, ib);
+    march<FIXED, MANNING, H, false>(T, it, wm, wm.ring, 0, nullptr, nullptr, ia, ib);
     __threadfence();
     __syncwarp();
     if (lane == 0) finish_item(T, ia, ib, true);
@@ -601,6 +638,79 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
   if (lane == 0) {
     __threadfence();
     if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x * kWarpsPerCta) {
+      a.work->next = 0u;
+      a.work->exited = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// The split tick: a CTA steps one 32 x 16 item at a time, its four warps four rows each (more
+// warps in flight where a tile has few items), the item's records from the CTA's shared ring.
+// The items are the 32 x 16 shape's.
+template <bool FIXED, bool MANNING>
+__global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const WarpMem<4> wm = warp_mem<4>(warp);
+  float* ring = warp_mem<4>(0).ring;     // the item's 16 rows of volumes
+  float* scratch = warp_mem<4>(1).ring;  // the ledger fold's slots
+  __shared__ uint32_t s_item, s_need;
+  __shared__ uint32_t s_ab[4];
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = atomicAdd(&a.work->next, 1u);
+      s_need = 0u;
+    }
+    if (threadIdx.x < 4) s_ab[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= a.n_items) break;
+    const uint32_t tile = item_tile_of(a.item_tile, item);
+    const TileDesc& T = a.tiles[tile];
+    const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
+    const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+    const TileCtl* ctl = T.ctl;
+    Item it;
+    it.cur = ctl->cur;
+    it.rec = ctl->rec;
+    const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
+    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
+    const bool src = (T.flags & kFlagSource) != 0u;
+    const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
+    it.apply_source = on ? 1u : 0u;
+    it.scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
+    it.X0 = int(bx) * kStrip;
+    const int Y0 = int(by) * 16;
+    it.Y0 = Y0 + 4 * warp;
+    if (local == 0u && warp == 1) {
+      fold_warp(T.rec[it.rec], T.groups_x * T.groups_y, scratch);
+      if (lane == 0) {
+        LedgerBits l = ctl->ledger;
+        ledger_update<FIXED>(l, scratch[0], scratch[kGroupCells], scratch[2 * kGroupCells], pa,
+                             pb, T.cfl, T.cell_m, a.max_dt);
+        T.ctl->ledger_next = l;
+      }
+      __syncwarp();
+    }
+    uint32_t ia = 0u, ib = 0u;
+    march<FIXED, MANNING, 4, true>(T, it, wm, ring, 4 * warp, s_ab, &s_need, ia, ib);
+    __threadfence();
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t ga = s_ab[lane < 16 ? 0 : 2], gb = s_ab[lane < 16 ? 1 : 3];
+      const uint32_t need = s_need;
+      group_records(T, T.rec[it.rec ^ 1u], it.X0, Y0 / 16, ga, gb, ring,
+                    it.dt > 0.0f && it.apply_source != 0u, (need & 1u) != 0u, (need & 2u) != 0u,
+                    ia, ib);
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) finish_item(T, ia, ib, true);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x) {
       a.work->next = 0u;
       a.work->exited = 0u;
       __threadfence();
@@ -812,6 +922,26 @@ __global__ void __launch_bounds__(256) flush_all_kernel(const TileDesc* tiles) {
   }
 }
 
+const void* split_fn(bool fixed, bool manning) {
+  if (fixed)
+    return manning ? (const void*)tick_split_kernel<true, true>
+                   : (const void*)tick_split_kernel<true, false>;
+  return manning ? (const void*)tick_split_kernel<false, true>
+                 : (const void*)tick_split_kernel<false, false>;
+}
+
+cudaError_t split_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = kWarpsPerCta * WarpMem<4>::kBytes;
+  if (fixed) {
+    if (manning) tick_split_kernel<true, true><<<grid, kCtaThreads, smem, s>>>(a);
+    else tick_split_kernel<true, false><<<grid, kCtaThreads, smem, s>>>(a);
+  } else {
+    if (manning) tick_split_kernel<false, true><<<grid, kCtaThreads, smem, s>>>(a);
+    else tick_split_kernel<false, false><<<grid, kCtaThreads, smem, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
 template <int H>
 const void* tick_fn(bool fixed, bool manning) {
   if (fixed)
@@ -855,6 +985,7 @@ size_t tick_smem_bytes(BlockShape shape) {
     case BlockShape::k32x16: return kWarpsPerCta * WarpMem<16>::kBytes;
     case BlockShape::k32x32: return kWarpsPerCta * WarpMem<32>::kBytes;
     case BlockShape::k32x64: return kWarpsPerCta * WarpMem<64>::kBytes;
+    case BlockShape::k32x16s: return kWarpsPerCta * WarpMem<4>::kBytes;
   }
   return 0;
 }
@@ -867,6 +998,7 @@ void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
     case BlockShape::k32x16: by = 16; return;
     case BlockShape::k32x32: by = 32; return;
     case BlockShape::k32x64: by = 64; return;
+    case BlockShape::k32x16s: by = 16; return;
   }
   by = 0;
 }
@@ -877,6 +1009,7 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning) {
     case BlockShape::k32x16: fn = tick_fn<16>(fixed, manning); break;
     case BlockShape::k32x32: fn = tick_fn<32>(fixed, manning); break;
     case BlockShape::k32x64: fn = tick_fn<64>(fixed, manning); break;
+    case BlockShape::k32x16s: fn = split_fn(fixed, manning); break;
   }
   const size_t smem = tick_smem_bytes(shape);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
@@ -893,6 +1026,7 @@ cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickAr
     case BlockShape::k32x16: return tick_launch<16>(fixed, manning, a, grid, s);
     case BlockShape::k32x32: return tick_launch<32>(fixed, manning, a, grid, s);
     case BlockShape::k32x64: return tick_launch<64>(fixed, manning, a, grid, s);
+    case BlockShape::k32x16s: return split_launch(fixed, manning, a, grid, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -900,7 +1034,8 @@ cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickAr
 cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaStream_t s) {
   if (a.n_items == 0) return cudaSuccess;
   switch (shape) {
-    case BlockShape::k32x16: return prime_launch<16>(fixed, a, s);
+    case BlockShape::k32x16:
+    case BlockShape::k32x16s: return prime_launch<16>(fixed, a, s);
     case BlockShape::k32x32: return prime_launch<32>(fixed, a, s);
     case BlockShape::k32x64: return prime_launch<64>(fixed, a, s);
   }

@@ -20,10 +20,10 @@ struct TickArgs {
   float max_dt;
 };
 
-// The block of cells one work item steps (32 columns by 16, 32 or 64 rows; 8 threads a row of
-// four). 32 x 32 is the default; the batched form's autotuner
-// chooses among all three.
-enum class BlockShape : uint8_t { k32x16 = 0, k32x32 = 1, k32x64 = 2 };
+// The block of cells one work item steps: 32 columns by 16, 32 or 64 rows, one warp marching
+// them; or (k32x16s) 32 by 16 split over a CTA's four warps, four rows each, for tiles with too
+// few items to fill the device. The batched form's autotuner chooses among all four.
+enum class BlockShape : uint8_t { k32x16 = 0, k32x32 = 1, k32x64 = 2, k32x16s = 3 };
 
 size_t tick_smem_bytes(BlockShape shape);
 int tick_threads(BlockShape shape);

@@ -9,7 +9,18 @@ water_live_device_tests.cpp:50-56, so the lattice is the same on every host), la
   plain_2048  2048 x 2048, H 50 m, depth U[0, 0.5] m, rain 1e-5 m a tick; 500 ticks.
   tiles_4096  4096 tiles, sides from {64, 96, 128, 192, 256, 384, 512}, each its own fBm (H 20 m)
               and a 2 m column of 32 x 32 at a seeded place; 200 ticks.
-  adjoint_512 512 x 512 and tiles_256_adjoint: see game_engine_gb300.adjoint.
+  adjoint_512 512 x 512, H 20 m, a lake: the surface at 21 m with a 0.05 m slosh and a centred
+              32 x 32 column 2 m higher, the source on at zero inflow (its gradient is taken
+              there); 2000 ticks, a checkpoint every 50; 64 probe cells, targets from a run on
+              the bed plus N(0, 0.1 m).
+  tiles_256_adjoint  256 tiles, sides from {64, 128, ..., 512}, each adjoint_512's lake on its
+              own fBm; 500 ticks, a checkpoint every 25; 64 probes a tile.
+
+The adjoint's lake is nowhere at rest: over a lake at rest every face's one-sided speeds tie
+exactly, where the scheme is not differentiable. It has no rain: rain of 1e-5 m a tick on 20 m of
+water is 5.2 units in the last place of an FP32 depth, so each tick rounds away a fixed share of
+it and the FP32 state drifts from the FP64 one by about 1e-3 m over 2000 ticks, a systematic
+difference between the two models that no gradient check within 1e-4 survives.
 """
 from __future__ import annotations
 
@@ -24,6 +35,10 @@ SEEDS = {
     "adjoint_512": 0x5EED_0004_C0FF_EE04,
     "tiles_256_adjoint": 0x5EED_0005_C0FF_EE05,
 }
+ADJOINT_TICKS, ADJOINT_EVERY = 2000, 50
+TILES_ADJOINT_TICKS, TILES_ADJOINT_EVERY = 500, 25
+PROBES = 64
+TARGET_NOISE_M = 0.1
 MAX_DT = 0.01  # the reference's rule dt = min(stable, max_dt) with a fixed max_dt
 MASK = 0xFFFFFFFF
 
@@ -157,3 +172,55 @@ def tiles_4096(count: int = 4096, sides=None, seed: int | None = None, with_bed:
         y0 = int(rng.integers(0, s - 32 + 1))
         out.append(Tile(s, s, bed, column(s, s, x0, y0), meta=dict(index=k)))
     return out
+
+
+def lake(nx, ny, bed, level=21.0, column_rise=2.0, phase=0.0):
+    """Depths of a lake over `bed`: the surface at `level` with a 0.05 m slosh and a centred
+    32 x 32 column `column_rise` higher."""
+    ys, xs = np.meshgrid(np.arange(ny, dtype=np.float64), np.arange(nx, dtype=np.float64),
+                         indexing="ij")
+    slosh = 0.05 * np.sin(xs / 2.9 + phase) * np.cos(ys / 3.3)
+    surf = (level + slosh).ravel() + column(nx, ny, nx // 2 - 16, ny // 2 - 16, depth=column_rise)
+    return np.maximum(surf - bed, 0.0)
+
+
+def probe_cells(cells: int, count: int, seed: int) -> np.ndarray:
+    """`count` distinct seeded cells, sorted (a partial Fisher-Yates on the reference's hash)."""
+    count = min(count, cells)
+    picked = {}
+    out = np.empty(count, dtype=np.uint32)
+    for k in range(count):
+        r = int(mix(np.uint64(k), np.uint64(seed & MASK))) % (cells - k)
+        j = k + r
+        out[k] = picked.get(j, j)
+        picked[j] = picked.get(k, k)
+    return np.sort(out)
+
+
+def adjoint_512(side: int = 512) -> Tile:
+    seed = SEEDS["adjoint_512"]
+    bed = fbm(side, side, 20.0, seed)
+    return Tile(side, side, bed, lake(side, side, bed), source=np.zeros(side * side),
+                meta=dict(ticks=ADJOINT_TICKS, every=ADJOINT_EVERY, max_dt=MAX_DT,
+                          name=f"adjoint_{side}",
+                          probes=probe_cells(side * side, PROBES, seed)))
+
+
+ADJOINT_TILE_SIDES = (64, 128, 192, 256, 320, 384, 448, 512)
+
+
+def tiles_256_adjoint(count: int = 256) -> list:
+    seed = SEEDS["tiles_256_adjoint"]
+    sides = tile_sides(count, seed, ADJOINT_TILE_SIDES)
+    out = []
+    for k, s in enumerate(sides):
+        bed = fbm(s, s, 20.0, seed + 7919 * (k + 1))
+        out.append(Tile(s, s, bed, lake(s, s, bed, phase=0.1 * k), source=np.zeros(s * s),
+                        meta=dict(index=k, probes=probe_cells(s * s, PROBES, seed + k))))
+    return out
+
+
+def perturbed_bed(bed: np.ndarray, seed: int, sigma: float = TARGET_NOISE_M) -> np.ndarray:
+    """The target run's bed: `bed` plus N(0, sigma) a cell (seeded)."""
+    rng = np.random.Generator(np.random.PCG64((seed >> 16) & 0xFFFFFFFF))
+    return bed + rng.normal(0.0, sigma, bed.size)

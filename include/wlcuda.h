@@ -192,8 +192,9 @@ typedef struct wl_tile {
   uint8_t west_open, east_open, south_open, north_open;
 } wl_tile;
 
-/* The launch's shape: rows of a 32-column work item (16, 32 or 64), the order items are dealt
- * (0 tiles by index, 1 the largest tiles first), and the trial's time a tick. */
+/* The launch's shape: the rows one warp marches down a 32-column work item (16, 32 or 64; or 4,
+ * 32 x 16 items split over four warps of a CTA), the order items are dealt (0 tiles by index, 1
+ * the largest tiles first), and the trial's time a tick. */
 typedef struct wl_tuning {
   uint32_t block_rows;
   uint32_t order;
@@ -250,6 +251,45 @@ int wl_batch_autotune(wl_batch* batch, float max_dt, uint32_t trial_ticks, wl_tu
 int wl_batch_set_tuning(wl_batch* batch, const wl_tuning* tuning, char* err, size_t err_len);
 int wl_batch_get_tuning(const wl_batch* batch, wl_tuning* out);
 wl_stream wl_batch_stream(wl_batch* batch);
+
+/* ---- the adjoint (no counterpart in the reference) --------------------------------------------
+ *
+ * For the loss L = sum over probe cells p of (h_T(p) - target_p)^2 after T ticks of fixed length
+ * max_dt from the current state, the gradients dL/d(bed) and dL/d(source_m_per_s) per cell. The
+ * sweep keeps the state every `every` ticks and recomputes each segment before its reverse ticks,
+ * so its device memory is (T/every + every + 2) states plus three bits a cell a tick; the
+ * gradients and the loss are accumulated in FP64. The forward ticks are the plain tick's
+ * arithmetic to the bit (a test holds the sweep's tick-T state to wl_run_steps's); no tick may be
+ * one the plain tick would shorten (wl_adjoint_read reports how many were). The sweep refuses
+ * (WL_ERR_REFUSED) fixed ops, Manning friction, the compensated source and a coarser source clock.
+ * A sweep reads its step's or batch's state, bed and source when it runs and changes none of them;
+ * destroy it before its step or batch. */
+typedef struct wl_adjoint wl_adjoint;
+
+/* Over a step: n_probes cells (y * nx + x) and their target depths. */
+int wl_adjoint_create(wl_step* step, uint32_t ticks, uint32_t every, uint32_t n_probes,
+                      const uint32_t* probes, const double* targets, wl_adjoint** out, char* err,
+                      size_t err_len);
+/* Over a batch: tile t's probes are probes[probe_first[t] .. probe_first[t + 1]) (tile-local cells),
+ * one loss a tile. */
+int wl_batch_adjoint_create(wl_batch* batch, uint32_t ticks, uint32_t every,
+                            const uint32_t* probe_first, const uint32_t* probes,
+                            const double* targets, wl_adjoint** out, char* err, size_t err_len);
+void wl_adjoint_destroy(wl_adjoint* adjoint);
+/* The whole sweep on the owner's stream (wl_step_stream / wl_batch_stream), no wait. */
+int wl_adjoint_enqueue(wl_adjoint* adjoint, float max_dt);
+/* The sweep (replayed from one captured CUDA graph when use_graph) and a wait for it. */
+int wl_adjoint_run(wl_adjoint* adjoint, float max_dt, int use_graph, char* err, size_t err_len);
+/* loss: one a tile; g_bed, g_source: every tile's cells, tile after tile (null to skip); limited:
+ * one count a tile of the ticks the plain tick would have shortened. */
+int wl_adjoint_read(wl_adjoint* adjoint, double* loss, double* g_bed, double* g_source,
+                    uint32_t* limited, char* err, size_t err_len);
+/* The state of tick T: three planes (h, hu, hv) a tile, tile after tile. */
+int wl_adjoint_read_final(wl_adjoint* adjoint, float* planes, char* err, size_t err_len);
+/* Kernel launches in one sweep, and the sweep's device bytes. */
+uint32_t wl_adjoint_launches(const wl_adjoint* adjoint);
+uint64_t wl_adjoint_device_bytes(const wl_adjoint* adjoint);
+
 
 #ifdef __cplusplus
 }  /* extern "C" */

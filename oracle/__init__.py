@@ -94,6 +94,25 @@ def lib():
         L.oracle_solver_state_hash.argtypes = [C.c_void_p]
         L.oracle_solver_volume.restype = C.c_double
         L.oracle_solver_volume.argtypes = [C.c_void_p]
+        _u32p = C.POINTER(C.c_uint32)
+        grid_args = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_double,
+                     C.c_uint32]
+        L.oracle_adj_forward.restype = C.c_uint32
+        L.oracle_adj_forward.argtypes = grid_args + [C.c_int, C.c_double, C.c_uint32, _dp, _dp,
+                                                     _dp, _dp]
+        L.oracle_adjoint.restype = C.c_uint32
+        L.oracle_adjoint.argtypes = grid_args + [C.c_int, C.c_double, C.c_uint32, _dp, _dp, _dp,
+                                                 _u32p, _dp, C.c_uint32, _dp, _dp, _dp]
+        L.oracle_adjoint_mixed.restype = C.c_uint32
+        L.oracle_adjoint_mixed.argtypes = grid_args + [C.c_double, C.c_uint32, _dp, _dp, _dp,
+                                                       _u32p, _dp, C.c_uint32, _dp, _dp, _dp]
+        L.oracle_adj_fd.restype = None
+        L.oracle_adj_fd.argtypes = grid_args + [C.c_double, C.c_uint32, _dp, _dp, _dp, _u32p, _dp,
+                                                C.c_uint32, _u32p, C.c_uint32, C.c_double,
+                                                C.c_double, _dp, _dp, C.c_uint32]
+        L.oracle_adj_loss64.restype = C.c_double
+        L.oracle_adj_loss64.argtypes = grid_args + [C.c_double, C.c_uint32, _dp, _dp, _dp, _u32p,
+                                                    _dp, C.c_uint32]
         _lib = L
     return _lib
 
@@ -340,6 +359,83 @@ class RefSolver:
 
     def volume(self):
         return ref().wsref_volume(self.h)
+
+
+# ---- the adjoint's checks --------------------------------------------------------------------
+
+def _grid_args(grid: Grid):
+    return (grid.nx, grid.ny, grid.cell_m, grid.gravity, grid.cfl, grid.dry_depth_m,
+            grid.open_edges)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def adj_forward(grid: Grid, dt, ticks, bed, source, state0, precision64=False):
+    """`ticks` ticks of fixed length `dt` (the adjoint's forward: native ops, no Manning, no
+    compensation, the source every step) from `state0` (3 planes: h, hu, hv). Returns the final
+    state (3, n) and the number of ticks the card would have shortened."""
+    bed, source, state0 = _keep(bed, source, state0)
+    out = np.zeros(3 * grid.cells)
+    lim = lib().oracle_adj_forward(*_grid_args(grid), int(precision64), float(dt), int(ticks),
+                                   _d(bed), _d(source), _d(state0), _d(out))
+    return out.reshape(3, -1), int(lim)
+
+
+def adjoint(grid: Grid, dt, ticks, bed, source, state0, probes, targets, precision64=True):
+    """The loss sum_p (h_T(p) - target_p)^2 and its gradients with respect to the bed and the
+    source by the reverse sweep. Returns (loss, g_bed, g_source, shortened ticks)."""
+    bed, source, state0, targets = _keep(bed, source, state0, targets)
+    probes = _u32(probes)
+    g_bed = np.zeros(grid.cells)
+    g_src = np.zeros(grid.cells)
+    loss = C.c_double(0.0)
+    lim = lib().oracle_adjoint(*_grid_args(grid), int(precision64), float(dt), int(ticks),
+                               _d(bed), _d(source), _d(state0),
+                               probes.ctypes.data_as(C.POINTER(C.c_uint32)), _d(targets),
+                               probes.size, C.byref(loss), _d(g_bed), _d(g_src))
+    return loss.value, g_bed, g_src, int(lim)
+
+
+def adjoint_mixed(grid: Grid, dt, ticks, bed, source, state0, probes, targets):
+    """The FP32 forward with the FP64 reverse sweep over it: (loss, g_bed, g_source, shortened)."""
+    bed, source, state0, targets = _keep(bed, source, state0, targets)
+    probes = _u32(probes)
+    g_bed = np.zeros(grid.cells)
+    g_src = np.zeros(grid.cells)
+    loss = C.c_double(0.0)
+    lim = lib().oracle_adjoint_mixed(*_grid_args(grid), float(dt), int(ticks), _d(bed),
+                                     _d(source), _d(state0),
+                                     probes.ctypes.data_as(C.POINTER(C.c_uint32)), _d(targets),
+                                     probes.size, C.byref(loss), _d(g_bed), _d(g_src))
+    return loss.value, g_bed, g_src, int(lim)
+
+
+def adj_fd(grid: Grid, dt, ticks, bed, source, state0, probes, targets, cells, eps_bed=1e-3,
+           rel_source=1e-3, threads=0, with_source=True):
+    """Central differences of the FP64 replay's loss at `cells`: on the bed and, when there is a
+    source and `with_source`, on the source."""
+    bed, source, state0, targets = _keep(bed, source, state0, targets)
+    probes, cells = _u32(probes), _u32(cells)
+    fd_bed = np.zeros(cells.size)
+    fd_src = np.zeros(cells.size) if (source is not None and with_source) else None
+    threads = threads or os.cpu_count() or 1
+    P = C.POINTER(C.c_uint32)
+    lib().oracle_adj_fd(*_grid_args(grid), float(dt), int(ticks), _d(bed), _d(source),
+                        _d(state0), probes.ctypes.data_as(P), _d(targets), probes.size,
+                        cells.ctypes.data_as(P), cells.size, float(eps_bed), float(rel_source),
+                        _d(fd_bed), _d(fd_src), int(threads))
+    return fd_bed, fd_src
+
+
+def adj_loss64(grid: Grid, dt, ticks, bed, source, state0, probes, targets):
+    bed, source, state0, targets = _keep(bed, source, state0, targets)
+    probes = _u32(probes)
+    return float(lib().oracle_adj_loss64(*_grid_args(grid), float(dt), int(ticks), _d(bed),
+                                         _d(source), _d(state0),
+                                         probes.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                         _d(targets), probes.size))
 
 
 def hash_floats(values) -> int:

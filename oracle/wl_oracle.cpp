@@ -1,7 +1,9 @@
 // ORACLE — test infrastructure only (see wl_oracle.hpp). A flat C ABI over the restatement, for
 // the tests' ctypes bindings (tests/oracle.py) and bench.py's CPU-baseline leg.
 #include "wl_oracle.hpp"
+#include "wl_adjoint.hpp"
 
+#include <atomic>
 #include <chrono>
 #include <cstdlib>
 #include <new>
@@ -218,5 +220,113 @@ void oracle_solver_ledger(void* p, double* out5) {
 }
 
 double oracle_solver_volume(void* p) { return static_cast<SolverHandle*>(p)->solver.surface_volume_m3(); }
+
+// ---- the adjoint's checks (wl_adjoint.hpp) ---------------------------------------------------
+
+// `ticks` fixed-length ticks from state0 (3 planes) into out (3 planes); returns the number of
+// ticks the card would have shortened.
+uint32_t oracle_adj_forward(uint32_t nx, uint32_t ny, double cell_m, double gravity, double cfl,
+                            double dry, uint32_t open_edges, int precision64, double dt,
+                            uint32_t ticks, const double* bed, const double* src,
+                            const double* state0, double* out) {
+  const Config c = make_config(nx, ny, cell_m, gravity, cfl, dry, open_edges);
+  const size_t n = size_t(nx) * ny;
+  auto run = [&](auto zero) {
+    using T = decltype(zero);
+    std::vector<T> b(n), s, a(3 * n), o(3 * n);
+    for (size_t i = 0; i < n; ++i) b[i] = T(bed[i]);
+    if (src) {
+      s.resize(n);
+      for (size_t i = 0; i < n; ++i) s[i] = T(src[i]);
+    }
+    for (size_t i = 0; i < 3 * n; ++i) a[i] = T(state0[i]);
+    uint32_t lim = 0;
+    for (uint32_t t = 0; t < ticks; ++t) {
+      if (limited<T>(c, T(dt), a.data())) ++lim;
+      forward_tick<T>(c, T(dt), b.data(), src ? s.data() : nullptr, a.data(), o.data(), nullptr);
+      a.swap(o);
+    }
+    for (size_t i = 0; i < 3 * n; ++i) out[i] = double(a[i]);
+    return lim;
+  };
+  return precision64 ? run(0.0) : run(0.0f);
+}
+
+// The loss and its gradients by the reverse sweep (the whole trajectory kept); returns the number
+// of shortened ticks.
+uint32_t oracle_adjoint(uint32_t nx, uint32_t ny, double cell_m, double gravity, double cfl,
+                        double dry, uint32_t open_edges, int precision64, double dt, uint32_t ticks,
+                        const double* bed, const double* src, const double* state0,
+                        const uint32_t* probes, const double* targets, uint32_t n_probes,
+                        double* loss, double* g_bed, double* g_src) {
+  const Config c = make_config(nx, ny, cell_m, gravity, cfl, dry, open_edges);
+  return precision64
+             ? adjoint<double>(c, dt, ticks, bed, src, state0, probes, targets, n_probes, loss,
+                               g_bed, g_src)
+             : adjoint<float>(c, dt, ticks, bed, src, state0, probes, targets, n_probes, loss,
+                              g_bed, g_src);
+}
+
+// The FP32 forward with the FP64 reverse sweep over it.
+uint32_t oracle_adjoint_mixed(uint32_t nx, uint32_t ny, double cell_m, double gravity, double cfl,
+                              double dry, uint32_t open_edges, double dt, uint32_t ticks,
+                              const double* bed, const double* src, const double* state0,
+                              const uint32_t* probes, const double* targets, uint32_t n_probes,
+                              double* loss, double* g_bed, double* g_src) {
+  const Config c = make_config(nx, ny, cell_m, gravity, cfl, dry, open_edges);
+  return adjoint_mixed(c, dt, ticks, bed, src, state0, probes, targets, n_probes, loss, g_bed,
+                       g_src);
+}
+
+// Central differences of the FP64 replay's loss: for each listed cell, (L(p + e) - L(p - e)) / 2e
+// with e = eps_bed on the bed and (when fd_src is not null and there is a source) e = rel_src *
+// |source| (eps_bed where the source is 0) on the source. The replays are dealt to `threads`
+// threads.
+void oracle_adj_fd(uint32_t nx, uint32_t ny, double cell_m, double gravity, double cfl, double dry,
+                   uint32_t open_edges, double dt, uint32_t ticks, const double* bed,
+                   const double* src, const double* state0, const uint32_t* probes,
+                   const double* targets, uint32_t n_probes, const uint32_t* cells,
+                   uint32_t n_cells, double eps_bed, double rel_src, double* fd_bed,
+                   double* fd_src, uint32_t threads) {
+  const Config c = make_config(nx, ny, cell_m, gravity, cfl, dry, open_edges);
+  const size_t n = size_t(nx) * ny;
+  const uint32_t jobs = n_cells * ((src && fd_src) ? 2u : 1u);
+  std::atomic<uint32_t> next{0};
+  auto worker = [&]() {
+    std::vector<double> b(bed, bed + n), s;
+    if (src) s.assign(src, src + n);
+    for (;;) {
+      const uint32_t j = next.fetch_add(1);
+      if (j >= jobs) break;
+      const bool on_src = j >= n_cells;
+      const uint32_t cell = cells[on_src ? j - n_cells : j];
+      std::vector<double>& p = on_src ? s : b;
+      const double base = p[cell];
+      const double e = on_src ? (base != 0.0 ? rel_src * std::fabs(base) : eps_bed) : eps_bed;
+      p[cell] = base + e;
+      const double lp = loss_fp64(c, dt, ticks, b.data(), src ? s.data() : nullptr, state0,
+                                  probes, targets, n_probes);
+      p[cell] = base - e;
+      const double lm = loss_fp64(c, dt, ticks, b.data(), src ? s.data() : nullptr, state0,
+                                  probes, targets, n_probes);
+      p[cell] = base;
+      (on_src ? fd_src : fd_bed)[on_src ? j - n_cells : j] = (lp - lm) / (2.0 * e);
+    }
+  };
+  const uint32_t nt = threads ? threads : 1u;
+  std::vector<std::thread> pool;
+  for (uint32_t t = 1; t < nt; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+}
+
+// The FP64 replay's loss alone.
+double oracle_adj_loss64(uint32_t nx, uint32_t ny, double cell_m, double gravity, double cfl,
+                         double dry, uint32_t open_edges, double dt, uint32_t ticks,
+                         const double* bed, const double* src, const double* state0,
+                         const uint32_t* probes, const double* targets, uint32_t n_probes) {
+  const Config c = make_config(nx, ny, cell_m, gravity, cfl, dry, open_edges);
+  return loss_fp64(c, dt, ticks, bed, src, state0, probes, targets, n_probes);
+}
 
 }  // extern "C"
