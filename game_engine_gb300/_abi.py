@@ -131,6 +131,9 @@ SIGNATURES = {
     "wl_adjoint_read_final": (C.c_int, [C.c_void_p, _fp, *_err]),
     "wl_adjoint_launches": (C.c_uint32, [C.c_void_p]),
     "wl_adjoint_device_bytes": (C.c_uint64, [C.c_void_p]),
+    # one tick that allocates nothing
+    "wl_tick_noalloc": (C.c_int, [C.POINTER(Config), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_float, wl_stream, *_err]),
 }
 
 

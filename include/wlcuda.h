@@ -290,6 +290,23 @@ int wl_adjoint_read_final(wl_adjoint* adjoint, float* planes, char* err, size_t 
 uint32_t wl_adjoint_launches(const wl_adjoint* adjoint);
 uint64_t wl_adjoint_device_bytes(const wl_adjoint* adjoint);
 
+/* ---- one tick that allocates nothing (no counterpart in the reference) ------------------------
+ *
+ * For callers that cannot allocate device memory (a frame loop that reserved its memory at
+ * start; a real-time thread): one plain tick of a caller-owned state, the records of `planes_in`
+ * first (prime_main), then one update of min(stable step, max_dt) into `planes_out`. Both hold
+ * four planes of nx * ny floats (h, hu, hv, remainder) on config->device; bed, and Manning's n and
+ * the source when not null (the source every step, no compensation), hold nx * ny floats there.
+ * `fixed_ops` selects Ops::fixed. The bytes are wl_run_steps's for one tick after wl_write_state
+ * of the same state. The scratch is a fixed device array holding at most 4096 groups of 16 x 16
+ * cells (1,048,576 cells as 1024 x 1024); a larger grid is refused with WL_ERR_SIZE. The first
+ * call on a device looks the array's address up (cudaGetSymbolAddress): make it before any stream
+ * capture. Enqueued on `stream` (null: the legacy default stream) without waiting. Calls share the
+ * array: two in flight at once on one device race, so a caller runs them one after another. */
+int wl_tick_noalloc(const wl_config* config, int fixed_ops, const float* planes_in,
+                    float* planes_out, const float* bed, const float* manning,
+                    const float* source, float max_dt, wl_stream stream, char* err,
+                    size_t err_len);
 
 #ifdef __cplusplus
 }  /* extern "C" */
