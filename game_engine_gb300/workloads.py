@@ -9,18 +9,21 @@ water_live_device_tests.cpp:50-56, so the lattice is the same on every host), la
   plain_2048  2048 x 2048, H 50 m, depth U[0, 0.5] m, rain 1e-5 m a tick; 500 ticks.
   tiles_4096  4096 tiles, sides from {64, 96, 128, 192, 256, 384, 512}, each its own fBm (H 20 m)
               and a 2 m column of 32 x 32 at a seeded place; 200 ticks.
-  adjoint_512 512 x 512, H 20 m, a lake: the surface at 21 m with a 0.05 m slosh and a centred
-              32 x 32 column 2 m higher, the source on at zero inflow (its gradient is taken
+  adjoint_512 512 x 512, H 2 m, a lake: the surface at 3 m with a 0.05 m slosh and a centred
+              32 x 32 column 1 m higher, the source on at zero inflow (its gradient is taken
               there); 2000 ticks, a checkpoint every 50; 64 probe cells, targets from a run on
               the bed plus N(0, 0.1 m).
   tiles_256_adjoint  256 tiles, sides from {64, 128, ..., 512}, each adjoint_512's lake on its
               own fBm; 500 ticks, a checkpoint every 25; 64 probes a tile.
 
 The adjoint's lake is nowhere at rest: over a lake at rest every face's one-sided speeds tie
-exactly, where the scheme is not differentiable. It has no rain: rain of 1e-5 m a tick on 20 m of
-water is 5.2 units in the last place of an FP32 depth, so each tick rounds away a fixed share of
-it and the FP32 state drifts from the FP64 one by about 1e-3 m over 2000 ticks, a systematic
-difference between the two models that no gradient check within 1e-4 survives.
+exactly, where the scheme is not differentiable. It is shallow and has no rain, because the
+gradient the sweep computes is the FP32 tick's, and the check is against FP64 differences:
+  - rain of 1e-5 m a tick on 20 m of water is 5.2 units in the last place of an FP32 depth, so
+    each tick rounds away a fixed share of it, and the FP32 state drifts from the FP64 one by
+    about 1e-3 m over 2000 ticks;
+  - without rain, a 20 m lake's FP32 rounding still moves the FP32 model's gradient 1.5e-4 away
+    from the FP64 model's over 2000 ticks; a 1-3 m lake's moves it 6e-5.
 """
 from __future__ import annotations
 
@@ -39,6 +42,7 @@ ADJOINT_TICKS, ADJOINT_EVERY = 2000, 50
 TILES_ADJOINT_TICKS, TILES_ADJOINT_EVERY = 500, 25
 PROBES = 64
 TARGET_NOISE_M = 0.1
+ADJOINT_RELIEF_M, ADJOINT_LEVEL_M, ADJOINT_RISE_M = 2.0, 3.0, 1.0
 MAX_DT = 0.01  # the reference's rule dt = min(stable, max_dt) with a fixed max_dt
 MASK = 0xFFFFFFFF
 
@@ -199,8 +203,9 @@ def probe_cells(cells: int, count: int, seed: int) -> np.ndarray:
 
 def adjoint_512(side: int = 512) -> Tile:
     seed = SEEDS["adjoint_512"]
-    bed = fbm(side, side, 20.0, seed)
-    return Tile(side, side, bed, lake(side, side, bed), source=np.zeros(side * side),
+    bed = fbm(side, side, ADJOINT_RELIEF_M, seed)
+    return Tile(side, side, bed, lake(side, side, bed, ADJOINT_LEVEL_M, ADJOINT_RISE_M),
+                source=np.zeros(side * side),
                 meta=dict(ticks=ADJOINT_TICKS, every=ADJOINT_EVERY, max_dt=MAX_DT,
                           name=f"adjoint_{side}",
                           probes=probe_cells(side * side, PROBES, seed)))
@@ -214,8 +219,9 @@ def tiles_256_adjoint(count: int = 256) -> list:
     sides = tile_sides(count, seed, ADJOINT_TILE_SIDES)
     out = []
     for k, s in enumerate(sides):
-        bed = fbm(s, s, 20.0, seed + 7919 * (k + 1))
-        out.append(Tile(s, s, bed, lake(s, s, bed, phase=0.1 * k), source=np.zeros(s * s),
+        bed = fbm(s, s, ADJOINT_RELIEF_M, seed + 7919 * (k + 1))
+        out.append(Tile(s, s, bed, lake(s, s, bed, ADJOINT_LEVEL_M, ADJOINT_RISE_M, phase=0.1 * k),
+                        source=np.zeros(s * s),
                         meta=dict(index=k, probes=probe_cells(s * s, PROBES, seed + k))))
     return out
 

@@ -176,3 +176,34 @@ def test_shortened_ticks_are_counted(gpu):
     assert limited[0] == want == 10
     a.close()
 
+
+def test_adjoint_configuration_against_central_differences(gpu):
+    """The full adjoint configuration (512 x 512, 2000 ticks, a checkpoint every 50, 64 probes)
+    against the FP64 replay's central differences at 32 cells (tests/golden/adjoint_512_fd.json,
+    made by make_adjoint_fd.py)."""
+    with open(os.path.join(GOLDEN, "adjoint_512_fd.json")) as f:
+        fd = json.load(f)
+    t = workloads.adjoint_512()
+    assert (t.nx, t.ny, t.meta["ticks"], t.meta["every"]) == (fd["nx"], fd["ny"], fd["ticks"],
+                                                             fd["every"])
+    dev = wl.DeviceStep()
+    assert dev.create(wl.Config(t.nx, t.ny, t.cell_m)), dev.error
+    assert dev.set_bed(t.bed) and dev.set_source(t.source)
+    assert dev.write_state(t.h, t.hu, t.hv)
+    a = Adjoint(dev, fd["ticks"], fd["every"], fd["probes"], fd["targets"])
+    a.run(fd["max_dt"])
+    loss, g_bed, g_src, limited = a.read()
+    assert limited[0] == 0
+    assert loss[0] == pytest.approx(fd["loss_fp64"], rel=1e-3)
+    cells = np.array(fd["fd_cells"])
+    err_bed = rel_err(g_bed[cells], fd["fd_bed"])
+    err_src = rel_err(g_src[cells], fd["fd_source"])
+    print(f"adjoint_512: bed {err_bed:.2e}, source {err_src:.2e} (max-norm relative, "
+          f"{cells.size} cells)")
+    assert err_bed < TOL
+    assert err_src < TOL
+    # the sweep's tick-2000 state is the plain tick's
+    fin = a.read_final().reshape(3, -1)
+    dev.run_steps(fd["ticks"], fd["max_dt"])
+    assert np.array_equal(bits(fin), bits(dev.read_state_bits().reshape(4, -1)[:3]))
+    a.close()
