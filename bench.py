@@ -221,11 +221,8 @@ def run_plain(args, tile, rank, world):
             flush_l2()
         torch.cuda.synchronize(dev)
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from game_engine_gb300.shard import max_over_ranks
+    ms = max_over_ranks(ms)  # the slowest rank's time (gloo or NCCL group under torchrun)
     launches = args.steps * (ticks + 2)
 
     # The dominant kernel's average launch, from the same events: every launch of a step but two

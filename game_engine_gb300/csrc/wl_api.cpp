@@ -110,7 +110,8 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
   if (s->options.stored_faces) s->flags |= WL_FLAG_STORED_FACES;
   t.open_edges = s->flags & 15u;
   // The block shape: 32 x 32, or the split 32 x 16 items where 32 x 32 items would leave the
-  // device short of warps (fewer than eight an SM); WLCUDA_BLOCK_ROWS (4, 16, 32 or 64) overrides.
+  // device short of warps (fewer than eight an SM); WLCUDA_BLOCK_ROWS (1, 4, 16, 32 or 64)
+  // overrides.
   wlc::BlockShape shape = wlc::BlockShape::k32x32;
   {
     int sms = 0;
@@ -121,6 +122,7 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
     if (sms > 0 && items32 < uint64_t(sms) * 8u) shape = wlc::BlockShape::k32x16s;
   }
   if (const char* rows = std::getenv("WLCUDA_BLOCK_ROWS")) {
+    if (std::strcmp(rows, "1") == 0) shape = wlc::BlockShape::k32x16b;
     if (std::strcmp(rows, "4") == 0) shape = wlc::BlockShape::k32x16s;
     if (std::strcmp(rows, "16") == 0) shape = wlc::BlockShape::k32x16;
     if (std::strcmp(rows, "32") == 0) shape = wlc::BlockShape::k32x32;

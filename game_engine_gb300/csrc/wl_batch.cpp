@@ -67,9 +67,11 @@ int cuda_fail(char* err, size_t len, const std::string& msg) {
 bool valid(const wl_batch* b) { return b != nullptr && b->set.valid(); }
 const char* k_no_device = "water_live: no device";
 
-// block_rows: the rows one warp marches (4: the 32 x 16 items split over a CTA's four warps).
+// block_rows: the rows one warp marches (4: the 32 x 16 items split over a CTA's four warps; 1: the
+// 32 x 16 items in three phases, no march).
 BlockShape shape_of_rows(uint32_t rows) {
-  return rows == 4    ? BlockShape::k32x16s
+  return rows == 1    ? BlockShape::k32x16b
+         : rows == 4  ? BlockShape::k32x16s
          : rows == 16 ? BlockShape::k32x16
          : rows == 64 ? BlockShape::k32x64
                       : BlockShape::k32x32;
@@ -493,7 +495,8 @@ int wl_batch_read_ledgers(wl_batch* b, wl_ledger* out, uint32_t count, char* err
 int wl_batch_set_tuning(wl_batch* b, const wl_tuning* t, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
   if (t == nullptr ||
-      (t->block_rows != 4 && t->block_rows != 16 && t->block_rows != 32 && t->block_rows != 64) ||
+      (t->block_rows != 1 && t->block_rows != 4 && t->block_rows != 16 && t->block_rows != 32 &&
+       t->block_rows != 64) ||
       t->order > 1)
     return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: a tuning out of range");
   std::string msg;
@@ -526,7 +529,7 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
     // writes is taken first and put back after.
     if (!b->set.snapshot(&msg)) return cuda_fail(err, err_len, msg);
     best.us_per_tick = std::numeric_limits<float>::infinity();
-    for (uint32_t rows : {4u, 16u, 32u, 64u}) {
+    for (uint32_t rows : {1u, 4u, 16u, 32u, 64u}) {
       for (uint32_t order : {0u, 1u}) {
         if (!b->set.reshape(shape_of_rows(rows), item_order(b->specs, order), &msg) ||
             !b->set.restore(&msg))

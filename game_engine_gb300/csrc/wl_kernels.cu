@@ -298,6 +298,94 @@ __device__ __forceinline__ float4 shfl_down4(const float4& v) {
                      __shfl_down_sync(0xffffffffu, v.z, 1), __shfl_down_sync(0xffffffffu, v.w, 1));
 }
 
+// One tick's per-cell constants of the update.
+struct UpdateCtx {
+  float g, dry, lam, area, edge_volume, dt, scale;
+  uint32_t flags;
+  int nx, ny;
+  bool src_on, comp, manning, any_open;
+};
+
+// update_main's per cell (slang:630-757): the four faces' fluxes into U' = U - dt/dx ((F_e - F_w)
+// + (F_n - F_s)), the clamp, the source (plain or compensated), Manning's friction and the dry
+// test. Gives h, hu, hv and the remainder, and adds the cell's source, open-edge and roundoff
+// volumes. `resid_in` is the cell's plane 3 (read when compensating), `nn` its Manning's n.
+template <bool FIXED>
+__device__ __forceinline__ void update_cell(const UpdateCtx& u, const float4& c, float hu, float hv,
+                                            float src, float resid_in, float nn, const float4& fw,
+                                            const float4& fe, const float4& fs, const float4& fn,
+                                            int gx, int gy, float& h, float& mu, float& mv,
+                                            float& residual, float& csrc, float& copn,
+                                            float& crnd) {
+  using O = Ops<FIXED>;
+  const uint32_t flags = u.flags;
+  if (u.any_open) {
+    if (gx == 0 && (flags & kFlagWestOpen)) copn = __fsub_rn(copn, __fmul_rn(fw.x, u.edge_volume));
+    if (gx + 1 == u.nx && (flags & kFlagEastOpen)) copn = __fadd_rn(copn, __fmul_rn(fe.x, u.edge_volume));
+    if (gy == 0 && (flags & kFlagSouthOpen)) copn = __fsub_rn(copn, __fmul_rn(fs.x, u.edge_volume));
+    if (gy + 1 == u.ny && (flags & kFlagNorthOpen)) copn = __fadd_rn(copn, __fmul_rn(fn.x, u.edge_volume));
+  }
+  const float lam = u.lam, area = u.area, dt = u.dt, scale = u.scale;
+  // U' = U - dt/dx ((F_e - F_w) + (F_n - F_s)) (slang:653-668)
+  h = __fsub_rn(c.x, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.x, fw.x), __fsub_rn(fn.x, fs.x))));
+  mu = __fsub_rn(hu, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.y, fw.z), __fsub_rn(fn.w, fs.w))));
+  mv = __fsub_rn(hv, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.w, fw.w), __fsub_rn(fn.y, fs.z))));
+  if (h < 0.0f) {
+    crnd = __fsub_rn(crnd, __fmul_rn(h, area));
+    h = 0.0f;
+  }
+  residual = 0.0f;
+  if (u.comp) residual = resid_in;
+  if (u.src_on && u.comp) {
+    const float owed = __fmul_rn(src, dt);
+    const float scaled = __fmul_rn(owed, scale);
+    const float target = __fadd_rn(scaled, residual);
+    float h2 = h;
+    if (target >= 0.0f) {
+      h2 = __fadd_rn(h, target);
+    } else {
+      const float want = -target;
+      const float taken = want < h ? want : h;
+      h2 = __fsub_rn(h, taken);
+    }
+    const float applied = __fsub_rn(h2, h);
+    const float left = __fsub_rn(target, applied);
+    residual = (h2 == 0.0f && target < 0.0f) ? 0.0f : left;
+    csrc = __fadd_rn(csrc, __fmul_rn(applied, area));
+    h = h2;
+  } else if (u.src_on) {
+    const float owed = __fmul_rn(src, dt);
+    const float added = __fmul_rn(owed, scale);
+    if (added >= 0.0f) {
+      h = __fadd_rn(h, added);
+      csrc = __fadd_rn(csrc, __fmul_rn(added, area));
+    } else {
+      const float want = -added;
+      const float taken = want < h ? want : h;
+      h = __fsub_rn(h, taken);
+      csrc = __fsub_rn(csrc, __fmul_rn(taken, area));
+    }
+  }
+  if (h >= u.dry) {
+    if (u.manning) {
+      // (hu)' = (hu)* / (1 + dt g n^2 |u*| / h^(4/3)) (slang:722-744)
+      const float g = u.g;
+      const float uu = O::div(mu, h);
+      const float vv = O::div(mv, h);
+      const float sp = O::sqrt(__fadd_rn(__fmul_rn(uu, uu), __fmul_rn(vv, vv)));
+      const float cb = O::cbrt(h);
+      const float k3 = __fmul_rn(__fmul_rn(__fmul_rn(g, nn), nn), sp);
+      const float k = O::div(k3, __fmul_rn(h, cb));
+      const float denom = __fadd_rn(1.0f, __fmul_rn(dt, k));
+      mu = O::div(mu, denom);
+      mv = O::div(mv, denom);
+    }
+  } else {
+    mu = 0.0f;
+    mv = 0.0f;
+  }
+}
+
 // The end of a split march: this warp's rows past the grid's edge hold nothing in the shared ring,
 // its largest speeds go to the item's two groups (s_ab: a, b of the west group, a, b of the east)
 // and the quantities some cell holds to s_need (1 open-edge, 2 roundoff).
@@ -456,6 +544,8 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   const bool any_open_band = (flags & 15u) != 0u;
   const float scale = it.scale;
   bool opn_seen = false, rnd_seen = false;
+  const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
+                     src_on, comp, manning, any_open_band};
 
   for (int j = 0; j < rows; ++j) {
     const int gy = Y0 + j;
@@ -487,70 +577,10 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
     float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
     float ax = 0.0f, ay = 0.0f;
     if (col) {
-      if (any_open_band) {
-        if (gx == 0 && (flags & kFlagWestOpen)) copn = __fsub_rn(copn, __fmul_rn(fw.x, edge_volume));
-        if (gx + 1 == nx && (flags & kFlagEastOpen)) copn = __fadd_rn(copn, __fmul_rn(fe.x, edge_volume));
-        if (gy == 0 && (flags & kFlagSouthOpen)) copn = __fsub_rn(copn, __fmul_rn(fs.x, edge_volume));
-        if (gy + 1 == ny && (flags & kFlagNorthOpen)) copn = __fadd_rn(copn, __fmul_rn(fn.x, edge_volume));
-      }
-      // U' = U - dt/dx ((F_e - F_w) + (F_n - F_s)) (slang:653-668)
-      float h = __fsub_rn(c.x, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.x, fw.x), __fsub_rn(fn.x, fs.x))));
-      float mu = __fsub_rn(hu, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.y, fw.z), __fsub_rn(fn.w, fs.w))));
-      float mv = __fsub_rn(hv, __fmul_rn(lam, __fadd_rn(__fsub_rn(fe.w, fw.w), __fsub_rn(fn.y, fs.z))));
-      if (h < 0.0f) {
-        crnd = __fsub_rn(crnd, __fmul_rn(h, area));
-        h = 0.0f;
-      }
-      float residual = 0.0f;
-      if (comp) residual = in[3 * n + i];
-      if (src_on && comp) {
-        const float owed = __fmul_rn(src, dt);
-        const float scaled = __fmul_rn(owed, scale);
-        const float target = __fadd_rn(scaled, residual);
-        float h2 = h;
-        if (target >= 0.0f) {
-          h2 = __fadd_rn(h, target);
-        } else {
-          const float want = -target;
-          const float taken = want < h ? want : h;
-          h2 = __fsub_rn(h, taken);
-        }
-        const float applied = __fsub_rn(h2, h);
-        const float left = __fsub_rn(target, applied);
-        residual = (h2 == 0.0f && target < 0.0f) ? 0.0f : left;
-        csrc = __fadd_rn(csrc, __fmul_rn(applied, area));
-        h = h2;
-      } else if (src_on) {
-        const float owed = __fmul_rn(src, dt);
-        const float added = __fmul_rn(owed, scale);
-        if (added >= 0.0f) {
-          h = __fadd_rn(h, added);
-          csrc = __fadd_rn(csrc, __fmul_rn(added, area));
-        } else {
-          const float want = -added;
-          const float taken = want < h ? want : h;
-          h = __fsub_rn(h, taken);
-          csrc = __fsub_rn(csrc, __fmul_rn(taken, area));
-        }
-      }
-      if (h >= dry) {
-        if (manning) {
-          // (hu)' = (hu)* / (1 + dt g n^2 |u*| / h^(4/3)) (slang:722-744)
-          const float nn = T.manning[i];
-          const float u = O::div(mu, h);
-          const float v = O::div(mv, h);
-          const float sp = O::sqrt(__fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)));
-          const float cb = O::cbrt(h);
-          const float k3 = __fmul_rn(__fmul_rn(__fmul_rn(g, nn), nn), sp);
-          const float k = O::div(k3, __fmul_rn(h, cb));
-          const float denom = __fadd_rn(1.0f, __fmul_rn(dt, k));
-          mu = O::div(mu, denom);
-          mv = O::div(mv, denom);
-        }
-      } else {
-        mu = 0.0f;
-        mv = 0.0f;
-      }
+      float h, mu, mv, residual;
+      update_cell<FIXED>(uc, c, hu, hv, src, comp ? in[3 * n + i] : 0.0f,
+                         manning ? T.manning[i] : 0.0f, fw, fe, fs, fn, gx, gy, h, mu, mv,
+                         residual, csrc, copn, crnd);
       qh[i] = h;
       qhu[i] = mu;
       qhv[i] = mv;
@@ -709,6 +739,267 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
     __syncthreads();
   }
   if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x) {
+      a.work->next = 0u;
+      a.work->exited = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// ---- the block tick -------------------------------------------------------------------------
+//
+// A CTA of 256 threads steps one 32 x 16 block (the 32 x 16 items, two 16 x 16 groups) at a time
+// in three phases through shared memory:
+//   1. the block's cells and a one-cell halo as {h, z, u, v} (ghosts at the tile's edges);
+//   2. every face of the block, one a thread (a face on the block's boundary is computed by both
+//      blocks that share it);
+//   3. every cell's update from its four faces, then the block's two records.
+// No thread's work waits on a row before it: a tile's faces are as many independent threads as the
+// device holds, where the march's warps walk their rows one after another.
+constexpr int kBlkW = 32, kBlkH = 16, kBlkThreads = 256;
+
+struct BlockSmem {
+  float4 cell[kBlkH + 2][kBlkW + 2];  // local (r, c) at [r + 1][c + 1]
+  float4 fx[kBlkH][kBlkW + 1];        // x face f of row r: between columns f - 1 and f
+  float4 fy[kBlkH + 1][kBlkW];        // y face f of column c: between rows f - 1 and f
+  float ring[3 * 16 * kStrip];        // the cells' source, open-edge and roundoff volumes
+  float fold[3 * kGroupCells];        // dt_main's fold (the tile's first block)
+  uint32_t item, need, ab[4];
+};
+
+template <bool FIXED, bool MANNING>
+__global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) {
+  extern __shared__ float4 smem_raw[];
+  BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (;;) {
+    if (t == 0) {
+      m.item = atomicAdd(&a.work->next, 1u);
+      m.need = 0u;
+    }
+    if (t < 4) m.ab[t] = 0u;
+    __syncthreads();
+    const uint32_t item = m.item;
+    if (item >= a.n_items) break;
+    const uint32_t tile = item_tile_of(a.item_tile, item);
+    const TileDesc& T = a.tiles[tile];
+    const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
+    const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+    const TileCtl* ctl = T.ctl;
+    const uint32_t cur = ctl->cur, rec = ctl->rec;
+    const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
+    const float dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
+    const bool src_flag = (T.flags & kFlagSource) != 0u;
+    const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
+    const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
+    const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
+    if (local == 0u && warp == 0) {
+      // dt_main's fold of the last update's records (slang:417-478), into the ledger's next copy.
+      fold_warp(T.rec[rec], T.groups_x * T.groups_y, m.fold);
+      if (lane == 0) {
+        LedgerBits l = ctl->ledger;
+        ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
+                             T.cfl, T.cell_m, a.max_dt);
+        T.ctl->ledger_next = l;
+      }
+      __syncwarp();
+    }
+    const int nx = int(T.nx), ny = int(T.ny);
+    const size_t n = size_t(T.nx) * T.ny;
+    const int rows = min(kBlkH, ny - Y0), cols = min(kBlkW, nx - X0);
+    const float* in = T.state[cur];
+    float* out = T.state[cur ^ 1u];
+    const float* bed = T.bed;
+    const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
+    const uint32_t flags = T.flags;
+    // The two cells this thread updates: (t >> 5, t & 31) and (8 + (t >> 5), t & 31).
+    const int cc = lane;
+    float rh[2], rhu[2], rhv[2];
+    bool live[2];
+    int gi[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int r = warp + 8 * k;
+      live[k] = r < rows && cc < cols;
+      gi[k] = (Y0 + r) * nx + X0 + cc;
+      rh[k] = rhu[k] = rhv[k] = 0.0f;
+      if (live[k]) {
+        rh[k] = in[gi[k]];
+        rhu[k] = in[n + gi[k]];
+        rhv[k] = in[2 * n + gi[k]];
+      }
+    }
+    uint32_t ga = 0u, gb = 0u;
+    bool opn_seen = false, rnd_seen = false;
+    if (!(dt > 0.0f)) {
+      // A step of no length: the state as it is, to the bit (slang:576-585).
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        if (live[k]) {
+          const int i = gi[k];
+          out[i] = rh[k];
+          out[n + i] = rhu[k];
+          out[2 * n + i] = rhv[k];
+          out[3 * n + i] = in[3 * n + i];
+          float ax, ay;
+          cell_speeds<FIXED>(g, dry, rh[k], rhu[k], rhv[k], ax, ay);
+          ga = max(ga, __float_as_uint(ax));
+          gb = max(gb, __float_as_uint(ay));
+        }
+      }
+    } else {
+      const float sw = (flags & kFlagWestOpen) ? 1.0f : -1.0f;
+      const float se = (flags & kFlagEastOpen) ? 1.0f : -1.0f;
+      const float ss = (flags & kFlagSouthOpen) ? 1.0f : -1.0f;
+      const float sn = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
+      // 1. the cells and the halo
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+        if (live[k])
+          m.cell[warp + 8 * k + 1][cc + 1] =
+              velocities<FIXED>(rh[k], rhu[k], rhv[k], bed[gi[k]], dry);
+      if (t < 2 * kBlkW + 2 * kBlkH) {
+        int r, c, gy, gx;  // the halo cell's local place and the global cell it reads
+        float4* slot;
+        bool ghost;
+        float sign = 1.0f;
+        bool flip_v = false;
+        bool need;
+        if (t < kBlkW) {  // south row
+          c = t;
+          r = -1;
+          need = c < cols;
+          ghost = Y0 == 0;
+          gy = ghost ? Y0 : Y0 - 1;
+          gx = X0 + c;
+          sign = ss;
+          flip_v = true;
+          slot = &m.cell[0][c + 1];
+        } else if (t < 2 * kBlkW) {  // north row
+          c = t - kBlkW;
+          r = rows;
+          need = c < cols;
+          ghost = Y0 + rows >= ny;
+          gy = ghost ? Y0 + rows - 1 : Y0 + rows;
+          gx = X0 + c;
+          sign = sn;
+          flip_v = true;
+          slot = &m.cell[rows + 1][c + 1];
+        } else if (t < 2 * kBlkW + kBlkH) {  // west column
+          r = t - 2 * kBlkW;
+          c = -1;
+          need = r < rows;
+          ghost = X0 == 0;
+          gy = Y0 + r;
+          gx = ghost ? X0 : X0 - 1;
+          sign = sw;
+          slot = &m.cell[r + 1][0];
+        } else {  // east column
+          r = t - 2 * kBlkW - kBlkH;
+          c = cols;
+          need = r < rows;
+          ghost = X0 + cols >= nx;
+          gy = Y0 + r;
+          gx = ghost ? X0 + cols - 1 : X0 + cols;
+          sign = se;
+          slot = &m.cell[r + 1][cols + 1];
+        }
+        if (need) {
+          const int i = gy * nx + gx;
+          float4 v = load_cell<FIXED>(in, in + n, in + 2 * n, bed, i, dry);
+          if (ghost) {
+            if (flip_v) v.w = __fmul_rn(sign, v.w);
+            else v.z = __fmul_rn(sign, v.z);
+          }
+          *slot = v;
+        }
+      }
+      __syncthreads();
+      // 2. the faces
+      const int nfx = rows * (cols + 1), nfy = (rows + 1) * cols;
+      const bool full = cols == kBlkW;
+      for (int q = t; q < nfx + nfy; q += kBlkThreads) {
+        if (q < nfx) {
+          const int r = full ? q / (kBlkW + 1) : q / (cols + 1);
+          const int f = q - r * (cols + 1);
+          m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
+        } else {
+          const int q2 = q - nfx;
+          const int f = full ? q2 / kBlkW : q2 / cols;
+          const int c = q2 - f * cols;
+          m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
+        }
+      }
+      __syncthreads();
+      // 3. the updates
+      const float cell_m = T.cell_m;
+      const float area = __fmul_rn(cell_m, cell_m);
+      const float lam = Ops<FIXED>::div(dt, cell_m);
+      const float edge_volume = __fmul_rn(dt, cell_m);
+      const bool comp = (flags & kFlagCompensate) != 0u;
+      const bool manning = MANNING && (flags & kFlagManning) != 0u;
+      const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
+                         apply, comp, manning, (flags & 15u) != 0u};
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int r = warp + 8 * k;
+        float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
+        if (live[k]) {
+          const int i = gi[k];
+          float h, mu, mv, residual;
+          update_cell<FIXED>(uc, m.cell[r + 1][cc + 1], rhu[k], rhv[k],
+                             apply ? T.source[i] : 0.0f, comp ? in[3 * n + i] : 0.0f,
+                             manning ? T.manning[i] : 0.0f, m.fx[r][cc], m.fx[r][cc + 1],
+                             m.fy[r][cc], m.fy[r + 1][cc], X0 + cc, Y0 + r, h, mu, mv, residual,
+                             csrc, copn, crnd);
+          out[i] = h;
+          out[n + i] = mu;
+          out[2 * n + i] = mv;
+          if (comp) out[3 * n + i] = residual;
+          float ax, ay;
+          cell_speeds<FIXED>(g, dry, h, mu, mv, ax, ay);
+          ga = max(ga, __float_as_uint(ax));
+          gb = max(gb, __float_as_uint(ay));
+        }
+        const int slot = r * kStrip + cc;
+        m.ring[slot] = csrc;
+        m.ring[16 * kStrip + slot] = copn;
+        m.ring[32 * kStrip + slot] = crnd;
+        opn_seen |= copn != 0.0f;
+        rnd_seen |= crnd != 0.0f;
+      }
+    }
+    // The block's two groups: their largest speeds and the quantities some cell holds.
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+      ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
+      gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
+    }
+    const bool any_opn = __any_sync(0xffffffffu, opn_seen);
+    const bool any_rnd = __any_sync(0xffffffffu, rnd_seen);
+    if ((lane & 15) == 0) {
+      atomicMax(&m.ab[(lane >> 4) * 2], ga);
+      atomicMax(&m.ab[(lane >> 4) * 2 + 1], gb);
+    }
+    if (lane == 0 && (any_opn || any_rnd))
+      atomicOr(&m.need, (any_opn ? 1u : 0u) | (any_rnd ? 2u : 0u));
+    __threadfence();
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t ia = 0u, ib = 0u;
+      const uint32_t need = m.need;
+      group_records(T, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[lane < 16 ? 0 : 2],
+                    m.ab[lane < 16 ? 1 : 3], m.ring, dt > 0.0f && apply, (need & 1u) != 0u,
+                    (need & 2u) != 0u, ia, ib);
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) finish_item(T, ia, ib, true);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
     __threadfence();
     if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x) {
       a.work->next = 0u;
@@ -930,6 +1221,26 @@ const void* split_fn(bool fixed, bool manning) {
                  : (const void*)tick_split_kernel<false, false>;
 }
 
+const void* block_fn(bool fixed, bool manning) {
+  if (fixed)
+    return manning ? (const void*)tick_block_kernel<true, true>
+                   : (const void*)tick_block_kernel<true, false>;
+  return manning ? (const void*)tick_block_kernel<false, true>
+                 : (const void*)tick_block_kernel<false, false>;
+}
+
+cudaError_t block_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
+  const size_t smem = sizeof(BlockSmem);
+  if (fixed) {
+    if (manning) tick_block_kernel<true, true><<<grid, kBlkThreads, smem, s>>>(a);
+    else tick_block_kernel<true, false><<<grid, kBlkThreads, smem, s>>>(a);
+  } else {
+    if (manning) tick_block_kernel<false, true><<<grid, kBlkThreads, smem, s>>>(a);
+    else tick_block_kernel<false, false><<<grid, kBlkThreads, smem, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t split_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
   const size_t smem = kWarpsPerCta * WarpMem<4>::kBytes;
   if (fixed) {
@@ -986,11 +1297,14 @@ size_t tick_smem_bytes(BlockShape shape) {
     case BlockShape::k32x32: return kWarpsPerCta * WarpMem<32>::kBytes;
     case BlockShape::k32x64: return kWarpsPerCta * WarpMem<64>::kBytes;
     case BlockShape::k32x16s: return kWarpsPerCta * WarpMem<4>::kBytes;
+    case BlockShape::k32x16b: return sizeof(BlockSmem);
   }
   return 0;
 }
 
-int tick_threads(BlockShape) { return kCtaThreads; }
+int tick_threads(BlockShape shape) {
+  return shape == BlockShape::k32x16b ? kBlkThreads : kCtaThreads;
+}
 
 void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
   bx = kStrip;
@@ -998,7 +1312,8 @@ void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
     case BlockShape::k32x16: by = 16; return;
     case BlockShape::k32x32: by = 32; return;
     case BlockShape::k32x64: by = 64; return;
-    case BlockShape::k32x16s: by = 16; return;
+    case BlockShape::k32x16s:
+    case BlockShape::k32x16b: by = 16; return;
   }
   by = 0;
 }
@@ -1010,12 +1325,14 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning) {
     case BlockShape::k32x32: fn = tick_fn<32>(fixed, manning); break;
     case BlockShape::k32x64: fn = tick_fn<64>(fixed, manning); break;
     case BlockShape::k32x16s: fn = split_fn(fixed, manning); break;
+    case BlockShape::k32x16b: fn = block_fn(fixed, manning); break;
   }
   const size_t smem = tick_smem_bytes(shape);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
     return 0;
   int blocks = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCtaThreads, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, tick_threads(shape), smem) !=
+      cudaSuccess)
     return 0;
   return blocks;
 }
@@ -1027,6 +1344,7 @@ cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickAr
     case BlockShape::k32x32: return tick_launch<32>(fixed, manning, a, grid, s);
     case BlockShape::k32x64: return tick_launch<64>(fixed, manning, a, grid, s);
     case BlockShape::k32x16s: return split_launch(fixed, manning, a, grid, s);
+    case BlockShape::k32x16b: return block_launch(fixed, manning, a, grid, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -1035,7 +1353,8 @@ cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaSt
   if (a.n_items == 0) return cudaSuccess;
   switch (shape) {
     case BlockShape::k32x16:
-    case BlockShape::k32x16s: return prime_launch<16>(fixed, a, s);
+    case BlockShape::k32x16s:
+    case BlockShape::k32x16b: return prime_launch<16>(fixed, a, s);
     case BlockShape::k32x32: return prime_launch<32>(fixed, a, s);
     case BlockShape::k32x64: return prime_launch<64>(fixed, a, s);
   }

@@ -222,7 +222,7 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
     return false;
   }
   for (BlockShape s : {BlockShape::k32x16, BlockShape::k32x32, BlockShape::k32x64,
-                       BlockShape::k32x16s})
+                       BlockShape::k32x16s, BlockShape::k32x16b})
     for (bool m : {false, true})
       if (tick_occupancy(s, fixed_, m) <= 0) {
         if (err) *err = "water_live: the tick kernel cannot be resident on this device";

@@ -192,9 +192,10 @@ typedef struct wl_tile {
   uint8_t west_open, east_open, south_open, north_open;
 } wl_tile;
 
-/* The launch's shape: the rows one warp marches down a 32-column work item (16, 32 or 64; or 4,
- * 32 x 16 items split over four warps of a CTA), the order items are dealt (0 tiles by index, 1
- * the largest tiles first), and the trial's time a tick. */
+/* The launch's shape: the rows one warp marches down a 32-column work item (16, 32 or 64; 4, 32 x
+ * 16 items split over four warps of a CTA; 1, 32 x 16 items stepped by a CTA in three phases
+ * through shared memory), the order items are dealt (0 tiles by index, 1 the largest tiles
+ * first), and the trial's time a tick. */
 typedef struct wl_tuning {
   uint32_t block_rows;
   uint32_t order;

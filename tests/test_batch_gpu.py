@@ -74,7 +74,7 @@ def test_per_tile_launches_give_the_same_bytes(gpu):
     assert np.array_equal(a.tile_hashes(), c.tile_hashes())
 
 
-@pytest.mark.parametrize("rows", [4, 16, 32, 64])
+@pytest.mark.parametrize("rows", [1, 4, 16, 32, 64])
 @pytest.mark.parametrize("order", [0, 1])
 def test_every_tuning_gives_the_same_bytes(gpu, rows, order):
     tiles, sides, edges = mixed_tiles()
@@ -97,7 +97,7 @@ def test_autotune_leaves_the_state_as_it_was(gpu):
     a.run_ticks(5, 0.02)
     b.run_ticks(5, 0.02)
     chosen = b.autotune(0.02, trial_ticks=3)
-    assert chosen["block_rows"] in (4, 16, 32, 64) and chosen["order"] in (0, 1)
+    assert chosen["block_rows"] in (1, 4, 16, 32, 64) and chosen["order"] in (0, 1)
     assert chosen["us_per_tick"] > 0
     a.run_ticks(9, 0.02)
     b.run_ticks(9, 0.02)

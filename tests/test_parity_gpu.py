@@ -26,7 +26,7 @@ def run_both(dev, ref, steps=None, advance=None, max_dt=INF):
     return steps
 
 
-@pytest.mark.parametrize("rows", [4, 16, 32, 64])
+@pytest.mark.parametrize("rows", [1, 4, 16, 32, 64])
 @pytest.mark.parametrize("fixed", [False, True])
 def test_count_of_water_bit_exact(gpu, rows, fixed):
     s = cases.slope(False)
@@ -68,7 +68,7 @@ def test_reference_cases_bit_exact(gpu, case):
 
 @pytest.mark.parametrize("nx,ny", [(1, 1), (1, 37), (45, 3), (17, 17), (33, 65), (100, 70),
                                    (31, 129)])
-@pytest.mark.parametrize("rows", [4, 16, 32, 64])
+@pytest.mark.parametrize("rows", [1, 4, 16, 32, 64])
 def test_odd_sizes_and_partial_blocks(gpu, nx, ny, rows):
     x, y = cases.grid_xy(nx, ny)
     bed = (cases.mix(x, y) % 100).astype(float) / 100.0
