@@ -109,17 +109,20 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
   if (config->north_open) s->flags |= WL_FLAG_NORTH_OPEN;
   if (s->options.stored_faces) s->flags |= WL_FLAG_STORED_FACES;
   t.open_edges = s->flags & 15u;
-  // The block shape: 32 x 32, or the split 32 x 16 items where 32 x 32 items would leave the
-  // device short of warps (fewer than eight an SM); WLCUDA_BLOCK_ROWS (1, 4, 16, 32 or 64)
+  // The block shape: the 32 x 16 march, or the three-phase 32 x 16 blocks where the march's
+  // 32 x 32 items would leave the device short of warps (fewer than eight an SM) and for the
+  // stored-faces form (the block form stores every face once, in shared memory, and gathers it:
+  // slang:483-551's order of work, the same bytes); WLCUDA_BLOCK_ROWS (1, 4, 16, 32 or 64)
   // overrides.
-  wlc::BlockShape shape = wlc::BlockShape::k32x32;
+  wlc::BlockShape shape = wlc::BlockShape::k32x16;
   {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, config->device) !=
         cudaSuccess)
       sms = 0;
     const uint64_t items32 = uint64_t((config->nx + 31u) / 32u) * ((config->ny + 31u) / 32u);
-    if (sms > 0 && items32 < uint64_t(sms) * 8u) shape = wlc::BlockShape::k32x16s;
+    if ((sms > 0 && items32 < uint64_t(sms) * 8u) || s->options.stored_faces)
+      shape = wlc::BlockShape::k32x16b;
   }
   if (const char* rows = std::getenv("WLCUDA_BLOCK_ROWS")) {
     if (std::strcmp(rows, "1") == 0) shape = wlc::BlockShape::k32x16b;

@@ -193,7 +193,7 @@ int wl_batch_create(const wl_config* common, const wl_options* options, const wl
     s.open_edges = (tiles[i].west_open ? 1u : 0u) | (tiles[i].east_open ? 2u : 0u) |
                    (tiles[i].south_open ? 4u : 0u) | (tiles[i].north_open ? 8u : 0u);
   }
-  b->tuning.block_rows = 32;
+  b->tuning.block_rows = 16;
   b->tuning.order = 1;
   b->tuning.us_per_tick = 0.0f;
   std::string msg;

@@ -104,13 +104,13 @@ extern "C" int wl_tick_noalloc(const wl_config* config, int fixed_ops, const flo
   StaticScratch* s = scratch_for(config->device, &msg);
   if (s == nullptr) return put(err, err_len, WL_ERR_CUDA, msg);
 
-  // The same shape rule as wl_create: split 32 x 16 items where 32 x 32 items would leave the
-  // device short of warps.
+  // The same shape rule as wl_create: three-phase blocks where the march's 32 x 32 items would
+  // leave the device short of warps, else the 32 x 16 march.
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, config->device) != cudaSuccess)
     return put(err, err_len, WL_ERR_CUDA, "water_live: the SM count");
   const uint64_t items32 = uint64_t((config->nx + 31u) / 32u) * ((config->ny + 31u) / 32u);
-  const BlockShape shape = items32 < uint64_t(sms) * 8u ? BlockShape::k32x16s : BlockShape::k32x32;
+  const BlockShape shape = items32 < uint64_t(sms) * 8u ? BlockShape::k32x16b : BlockShape::k32x16;
   uint32_t bx = 0, by = 0;
   block_dims(shape, bx, by);
 

@@ -12,7 +12,7 @@ import pytest
 
 import cases
 import oracle
-from pairs import config
+from pairs import block_rows, config
 from game_engine_gb300 import water_live as wl
 
 pytestmark = pytest.mark.gpu
@@ -190,10 +190,13 @@ def test_water_is_counted_as_the_reference_counts_it(gpu, all_open, fixed):
 
 @pytest.mark.parametrize("fixed", [False, True])
 def test_same_bytes_twice_and_stored_faces(gpu, fixed):
+    # The stored-faces form (every face stored once, then gathered: the block shape) against the
+    # march, twice.
     c = cases.slope(False)
     hashes = []
-    for stored in (False, False, True):
-        s = device(c, fixed, stored_faces=stored)
+    for stored, rows in ((False, 16), (False, 16), (True, None)):
+        with block_rows(rows):
+            s = device(c, fixed, stored_faces=stored)
         assert s.run_steps(400, INF)
         hashes.append(s.state_hash())
     assert hashes[0] != 0
