@@ -92,3 +92,28 @@ def test_an_empty_grid_is_refused(wl_lib):
     assert wl_lib.wl_create(C.byref(cfg), None, C.byref(out), err, 128) == 2
     assert b"empty grid" in err.value
     assert not out.value
+
+
+def test_the_numerics_policy_of_every_build():
+    # The reference's contraction sanitizer (water_live_tests.cpp:57-105) checks its SPIR-V for
+    # contracted float operations. Here the same policy is held at the build: every translation
+    # unit of the tick compiles with no contraction and IEEE division and square root, the host
+    # code and the oracle with -ffp-contract=off. The adjoint's unit alone takes contraction (its
+    # reverse march is a derivative held to a tolerance; its forward is spelled in _rn intrinsics).
+    from game_engine_gb300 import buildlib
+    for src in buildlib.SOURCES:
+        flags = buildlib.NUMERICS_BY_SOURCE.get(src, buildlib.NUMERICS)
+        assert "-prec-div=true" in flags and "-prec-sqrt=true" in flags and "-ftz=false" in flags
+        if src != "wl_adjoint.cu":
+            assert "--fmad=false" in flags, src
+    assert "-ffp-contract=off" in ",".join(buildlib.HOST)
+    make = open(os.path.join(ROOT, "oracle", "Makefile")).read()
+    assert "-ffp-contract=off" in make and "-fno-fast-math" in make
+    # the adjoint's forward march spells every + - * / of the update in correctly rounded
+    # intrinsics: no bare float operator on its lines
+    src = open(os.path.join(ROOT, "game_engine_gb300", "csrc", "wl_adjoint.cu")).read()
+    fwd = src[src.index("__device__ void forward_march("):src.index("// ---- the reverse march")]
+    update = fwd[fwd.index("float h = __fsub_rn("):fwd.index("out[i] = h;")]
+    code = re.sub(r"//[^\n]*", "", update)
+    assert not re.search(r"[\w)\]]\s*[-+*/]\s*[\w(]", re.sub(r"__f\w+_rn\(|\b\d+\.\d+f\b", "", code)
+                         .replace("-added", "").replace("-target", "")), "a bare float operator"

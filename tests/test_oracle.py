@@ -145,3 +145,17 @@ def test_advance_refuses_a_coarser_source_clock(oracle_mod):
     s.set_source(c["source"], every=8)
     steps, refused = s.advance(1.0)
     assert steps == 0 and refused
+
+
+def test_solver64_thread_count_invariance(oracle_mod):
+    # water_state_tests.cpp:739-760: the bytes do not depend on how many threads step the rows.
+    c = cases.slope(False)
+    hashes = []
+    for threads in (1, 3, 8):
+        s = oracle_mod.Solver64(oracle_mod.Grid(c["nx"], c["ny"], c["cell_m"], open_edges=2),
+                                threads)
+        s.set_state(c["h"])
+        s.set_inputs(c["bed"], c["manning"], c["source"])
+        s.advance(5.0)
+        hashes.append(s.state_hash())
+    assert hashes[0] == hashes[1] == hashes[2] != 0
