@@ -131,6 +131,21 @@ def cpu_baseline(tile, threads: int, budget_s: float = 12.0):
                       f"reference CPU tick restated in oracle/, {threads} threads"}
 
 
+def workload_config(tile, ticks: int, world: int) -> dict:
+    """The `config` both arms print for a plain-tick workload."""
+    per_tick = tile.cells * (32.125 if tile.source is not None else 28.125)
+    return {
+        "workload": f"plain tick {tile.nx}x{tile.ny} from the same seeded initial state, closed "
+                    f"edges, max_dt {tile.meta.get('max_dt', 0.01)} s"
+                    + (", rain" if tile.source is not None else ""),
+        "cells": tile.cells, "ticks_per_step": ticks, "max_dt": tile.meta.get("max_dt", 0.01),
+        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+        "l2": f"{per_tick / 1e6:.1f} MB of planes a tick "
+              f"({'larger' if per_tick > 129e6 else 'smaller'} than the 129 MB L2); a 512 MB "
+              "write flushes L2 between steps, outside the timed events",
+    }
+
+
 def run_reference(args, tile, rank, world):
     """--impl reference: the reference CPU tick on this host's cores, on rank 0 only."""
     if rank != 0:
@@ -159,9 +174,9 @@ def run_reference(args, tile, rank, world):
         "impl": "reference", "metric": "water cell-updates/s", "value": value,
         "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fBm terrain)",
-        "config": {"workload": tile.meta.get("name"), "cells": tile.cells,
-                   "ticks_per_step": ticks_per_step},
+        "vs_baseline": None, "dtype": "f64", "data": tile.meta.get("data", "synthetic"),
+        "config": dict(workload_config(tile, ticks_per_step, world),
+                       parallelism="the host's cores, rank 0"),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
@@ -283,15 +298,9 @@ def run_plain(args, tile, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded 6-octave fBm terrain 0-50 m, depth U[0,0.5] m, rain 1e-5 m/tick",
-        "config": {"workload": f"plain tick {tile.nx}x{tile.ny}, {ticks} ticks from the same "
-                               "initial state, closed edges, max_dt 0.01 s",
-                   "cells": n, "ticks_per_step": ticks, "max_dt": max_dt,
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (8 planes of 16.8 MB = 134 MB per tick) and an "
-                         "L2 flush (512 MB write) between steps, outside the timed events",
-                   "cfl_limited_ticks": None,
-                   "ledger_steps_last_run": ledger["steps"] if ledger else None},
+        "data": tile.meta.get("data", "synthetic"),
+        "config": dict(workload_config(tile, ticks, world),
+                       ledger_steps_last_run=ledger["steps"] if ledger else None),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes_per_launch": algo_bytes,

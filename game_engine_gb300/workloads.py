@@ -144,7 +144,9 @@ def plain_256() -> Tile:
     n = 256
     bed = fbm(n, n, 20.0, SEEDS["plain_256"])
     h = column(n, n, n // 2 - 16, n // 2 - 16)
-    return Tile(n, n, bed, h, meta=dict(ticks=1000, max_dt=MAX_DT, name="plain_256"))
+    return Tile(n, n, bed, h, meta=dict(ticks=1000, max_dt=MAX_DT, name="plain_256",
+                                        data="synthetic: seeded 6-octave fBm terrain 0-20 m, "
+                                             "dry but a centred 32 x 32 column of 2 m"))
 
 
 def plain_2048(side: int = 2048) -> Tile:
@@ -153,7 +155,9 @@ def plain_2048(side: int = 2048) -> Tile:
     h = rng.uniform(0.0, 0.5, side * side)
     rain = np.full(side * side, 1e-5 / MAX_DT)  # 1e-5 m a tick at dt = max_dt
     return Tile(side, side, bed, h, source=rain,
-                meta=dict(ticks=500, max_dt=MAX_DT, name=f"plain_{side}"))
+                meta=dict(ticks=500, max_dt=MAX_DT, name=f"plain_{side}",
+                          data="synthetic: seeded 6-octave fBm terrain 0-50 m, depth U[0, 0.5] m, "
+                               "rain 1e-5 m a tick"))
 
 
 TILE_SIDES = (64, 96, 128, 192, 256, 384, 512)
