@@ -166,6 +166,27 @@ def test_the_sweep_refuses_what_it_does_not_differentiate(gpu):
         Adjoint(dev, 0, 5, probes, targets)
 
 
+def test_repeated_probes_and_a_single_tick(gpu):
+    # A probe listed twice counts twice (the loss and the seed add in probe order); T = 1 and
+    # k = 1 are the smallest sweep.
+    c = basin(30, 22, 6, edges=10)
+    for ticks, every in ((1, 1), (9, 2)):
+        probes = np.array([7, 7, 100, 651], np.uint32)
+        fin, _ = oracle.adj_forward(grid(c), DT, ticks, c["bed"], c["source"], c["state0"],
+                                    precision64=True)
+        targets = fin[0][probes] + np.array([0.01, -0.02, 0.03, 0.0])
+        dev = device_step(c)
+        a = Adjoint(dev, ticks, every, probes, targets)
+        a.run(DT)
+        loss, g_bed, g_src, limited = a.read()
+        l32, b32, s32, _ = oracle.adjoint(grid(c), DT, ticks, c["bed"], c["source"],
+                                          c["state0"], probes, targets, precision64=False)
+        assert limited[0] == 0
+        assert loss[0] == pytest.approx(l32, rel=1e-12)
+        assert rel_err(g_bed, b32) < 1e-5 and rel_err(g_src, s32) < 1e-5
+        a.close()
+
+
 def test_shortened_ticks_are_counted(gpu):
     c = basin(20, 16, 1, level=30.0)
     dev = device_step(c)
