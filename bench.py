@@ -347,13 +347,16 @@ def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
         torch.cuda.synchronize(dev)
         ms += ev[0].elapsed_time(ev[1])
     batched = cells * ticks * steps / (ms * 1e-3)
-    # The per-tile-launch form on the same tiles, given its best shape (16-row items, the most
-    # parallel) and timed three ways: one stream, one stream from a captured graph, and tiles
-    # dealt to 64 concurrent streams as independent steps would run. Fewer ticks: it is slow.
+    # The per-tile-launch form on the same tiles, timed four ways: 16-row marches on one stream,
+    # from a captured graph, and dealt to 64 concurrent streams as independent steps would run;
+    # and the three-phase blocks (the small-tile shape) on 64 streams. The best of them is the
+    # comparison. Fewer ticks: it is slow.
     per_ticks = 10
-    b.set_tuning(16, 0)
     per = {}
-    for name, graph, nstreams in (("stream", False, 1), ("graph", True, 1), ("streams_64", False, 64)):
+    for name, graph, nstreams, rows in (("stream", False, 1, 16), ("graph", True, 1, 16),
+                                        ("streams_64", False, 64, 16),
+                                        ("streams_64_blocks", False, 64, 1)):
+        b.set_tuning(rows, 0)
         b.write_state(h0)
         b.run_tile_ticks(2, workloads.MAX_DT, graph=graph, streams=nstreams)
         ev[0].record(stream)
@@ -369,7 +372,7 @@ def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
         "cells": cells, "tiles": count, "value": batched, "unit": "cell-updates/s",
         "ms_per_tick": ms / (steps * ticks), "tuning": tuning,
         "per_tile_launch": {"value": per_tile, "unit": "cell-updates/s", "forms": per,
-                            "block_rows": 16},
+                            "best": max(per, key=per.get)},
         "speedup_vs_per_tile_launch": batched / per_tile,
         "launches_per_tick": {"batched": 1, "per_tile": count},
     }
@@ -521,6 +524,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched and adjoint measurements beside the headline")
+    ap.add_argument("--tiles", type=int, default=4096,
+                    help="tiles of the batched workload (a smaller batch for a profiler; the "
+                         "configuration's number is measured with the default)")
     ap.add_argument("--ticks", type=int, default=0,
                     help="ticks a step instead of the workload's (a short run for a profiler; "
                          "the configuration's number is measured with the default)")
@@ -535,7 +541,10 @@ def main():
         if rank == 0:
             fn = {"tiles_4096": run_tiles, "adjoint_512": run_adjoint,
                   "tiles_256_adjoint": run_tiles_adjoint}[args.workload]
-            out = fn(args.steps, args.warmup, args.ticks)
+            if args.workload == "tiles_4096":
+                out = run_tiles(args.steps, args.warmup, args.ticks, count=args.tiles)
+            else:
+                out = fn(args.steps, args.warmup, args.ticks)
             print(json.dumps(out), flush=True)
         return
     if args.workload == "plain_2048":

@@ -222,7 +222,10 @@ __device__ __forceinline__ void cell_speeds(float g, float dry, float h, float h
   const bool wet = h >= dry;
   const float u = wet ? O::div(hu, h) : 0.0f;
   const float v = wet ? O::div(hv, h) : 0.0f;
-  const float c = O::sqrt(__fmul_rn(g, h));
+  // sqrt(+-0) is +-0: a dry cell's zero takes no square root (the intrinsic's special-case path
+  // is its slow one, and most cells of a dry landscape are exactly zero).
+  const float gh = __fmul_rn(g, h);
+  const float c = gh == 0.0f ? gh : O::sqrt(gh);
   ax = __fadd_rn(fabsf(u), c);
   ay = __fadd_rn(fabsf(v), c);
 }

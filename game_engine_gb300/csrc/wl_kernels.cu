@@ -24,6 +24,11 @@
 //   - The last item of a tile to finish commits the tick: the new ledger, the flipped copy and
 //     record buffer, the new largest speeds and the source's clock.
 //
+// Two other shapes share the items, the update (update_cell) and the commit: the split march
+// (tick_split_kernel: a 32 x 16 item by a CTA's four warps, four rows each, for small tiles) and
+// the block tick (tick_block_kernel: a 32 x 16 item by 256 threads in three phases through shared
+// memory; the small-tile default and the stored-faces form). Every shape gives the same bytes.
+//
 // HBM traffic per cell-update: h, hu, hv, bed read (+ source, + Manning's n, + the remainder when
 // on), h, hu, hv written (+ the remainder), a 32-byte record per 256 cells.
 #include "wl_device.cuh"
