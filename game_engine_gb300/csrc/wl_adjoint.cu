@@ -440,6 +440,12 @@ __device__ void reverse_march(const AdjTile& A, const float* U, const float* lam
   for (int j = 0; j < rows; ++j) {
     const int gy = Y0 + j;
     const bool nghost = gy + 1 >= ny;
+    // This row's running gradients, read now so the read is in flight while the row computes.
+    double gbed = 0.0, gsrc = 0.0;
+    if (col) {
+      gbed = A.g_bed[i];
+      gsrc = A.g_src[i];
+    }
     float4 nc, nm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (!nghost) {
       nc = cell_state(nh, nhu, nhv, nz, dry);
@@ -501,8 +507,8 @@ __device__ void reverse_march(const AdjTile& A, const float* U, const float* lam
       lam_out[i] = lh;
       lam_out[n + i] = lu;
       lam_out[2 * n + i] = lv;
-      A.g_bed[i] += double(acc.y);
-      A.g_src[i] += double(cm.w) * ddt;
+      A.g_bed[i] = gbed + double(acc.y);
+      A.g_src[i] = gsrc + double(cm.w) * ddt;
     }
     c = nc;
     cm = nm;
