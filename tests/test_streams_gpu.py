@@ -91,3 +91,23 @@ def test_plain_2048_full_run_properties(gpu):
     involved = before + abs(led["source_m3"])
     assert abs(balance) <= 500 * 2.0 ** -24 * involved
     assert led["source_m3"] > 0
+
+
+def test_a_wait_past_its_limit_is_a_timeout_and_the_step_stays_usable(gpu, monkeypatch):
+    # Failure detection without a fault: every wait on the device has a limit (WLCUDA_WAIT_S).
+    # A wait that passes it returns WL_ERR_TIMEOUT's message, nothing hangs, and the work it
+    # waited for finishes; the next call waits for it and the bytes are those of the whole run.
+    t = workloads.plain_2048(1024)
+    ref = wl.DeviceStep()
+    assert ref.create(wl.Config(t.nx, t.ny, t.cell_m))
+    ref.set_bed(t.bed), ref.set_source(t.source), ref.write_state(t.h, t.hu, t.hv)
+    assert ref.run_steps(300, workloads.MAX_DT)
+    want = ref.state_hash()
+    dev = wl.DeviceStep()
+    assert dev.create(wl.Config(t.nx, t.ny, t.cell_m))
+    dev.set_bed(t.bed), dev.set_source(t.source), dev.write_state(t.h, t.hu, t.hv)
+    monkeypatch.setenv("WLCUDA_WAIT_S", "0.000001")
+    assert not dev.run_steps(300, workloads.MAX_DT)
+    assert "wait limit" in dev.error
+    monkeypatch.delenv("WLCUDA_WAIT_S")
+    assert dev.state_hash() == want
