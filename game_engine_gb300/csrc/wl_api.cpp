@@ -67,7 +67,7 @@ int flush(wl_step* s, wl_ledger_bits* bits, std::string* msg) {
   if (!s->set.length_pass(0, 0.0f, msg)) return WL_ERR_CUDA;
   wlc::TileCtl c;
   if (!s->set.read_ctl(0, c, msg)) return WL_ERR_CUDA;
-  std::memcpy(bits, &c.ledger, sizeof *bits);
+  std::memcpy(bits, &c.ledger[c.rec & 1u], sizeof *bits);
   return WL_OK;
 }
 
@@ -337,7 +337,7 @@ int wl_read_ledger_bits(wl_step* s, wl_ledger_bits* out, char* err, size_t err_l
   wlc::TileCtl c;
   std::string msg;
   if (!s->set.read_ctl(0, c, &msg)) return cuda_fail(err, err_len, msg);
-  std::memcpy(out, &c.ledger, sizeof *out);
+  std::memcpy(out, &c.ledger[c.rec & 1u], sizeof *out);
   return WL_OK;
 }
 

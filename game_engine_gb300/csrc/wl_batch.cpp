@@ -481,7 +481,7 @@ int wl_batch_read_ledgers(wl_batch* b, wl_ledger* out, uint32_t count, char* err
   if (!b->set.flush_all(&msg) || !b->set.read_all_ctl(ctl.data(), &msg))
     return cuda_fail(err, err_len, msg);
   for (uint32_t t = 0; t < count; ++t) {
-    const wlc::LedgerBits& l = ctl[t].ledger;
+    const wlc::LedgerBits& l = ctl[t].ledger[ctl[t].rec & 1u];
     out[t].source_m3 = double(l.source_hi) + double(l.source_lo);
     out[t].open_edge_out_m3 = double(l.open_hi) + double(l.open_lo);
     out[t].roundoff_m3 = double(l.roundoff_hi) + double(l.roundoff_lo);

@@ -42,22 +42,26 @@ static_assert(sizeof(LedgerBits) == 48, "WaterLedger is 48 bytes");
 
 // A tile's control block, all of a tick's state that is not a plane: the ledger as the reference
 // keeps it, which copy holds the state, which record buffer holds the last update's records, the
-// last update's largest speeds (the next step's length is chosen from them), and the source's
-// clock. Every launch reads it and the tile's last work item rewrites it, so a captured graph of
-// ticks replays correctly any number of times.
+// largest speeds of each record buffer's update (the next step's length is chosen from them), and
+// the source's clock. Every launch reads it and the tile's last work item flips it, so a captured
+// graph of ticks replays correctly any number of times.
+//
+// The ledger and the largest speeds come in two slots indexed like the record buffers. A launch
+// reads slot `rec` and writes slot `rec ^ 1` (the ledger by the tile's first item, the speeds by
+// every item's atomicMax), and the last item flips `rec`. Nothing a launch writes is read in the
+// same launch, so no item orders its writes before its `done` count: the next launch sees them
+// all at the kernel boundary. Between launches the speeds of slot `rec ^ 1` are zero; the last
+// item keeps that true by clearing slot `rec` (every item of the tile has read it by then).
 struct TileCtl {
-  LedgerBits ledger;       // 0: the ledger (read_ledger_bits copies these 48 bytes)
-  LedgerBits ledger_next;  // 48: this tick's ledger, committed by the tile's last work item
-  uint32_t cur;            // 96: the copy that holds the state
-  uint32_t rec;            // 100: the record buffer that holds the last update's records
-  uint32_t prev_a;         // 104: largest |u| + c of the last update (float bits, never -0)
-  uint32_t prev_b;         // 108: largest |v| + c
-  uint32_t max_a;          // 112: this tick's running maxima (atomicMax on the bits)
-  uint32_t max_b;          // 116
-  uint32_t done;           // 120: work items of this tile finished in this launch
-  uint32_t src_phase;      // 124: steps since the source last applied (set_source's clock)
-  uint32_t error;          // 128: a device error word (0: none)
-  uint32_t ticks;          // 132: launches that stepped this tile (a diagnosis counter)
+  LedgerBits ledger[2];  // 0, 48: the ledger; ledger[rec] is the current one
+  uint32_t cur;          // 96: the copy that holds the state
+  uint32_t rec;          // 100: the record buffer that holds the last update's records
+  uint32_t max_a[2];     // 104: largest |u| + c of the update whose records are rec[k] (bits)
+  uint32_t max_b[2];     // 112: largest |v| + c
+  uint32_t done;         // 120: work items of this tile finished in this launch
+  uint32_t src_phase;    // 124: steps since the source last applied (set_source's clock)
+  uint32_t error;        // 128: a device error word (0: none)
+  uint32_t ticks;        // 132: launches that stepped this tile (a diagnosis counter)
   uint32_t pad[2];
 };
 static_assert(sizeof(TileCtl) == 144, "TileCtl layout");

@@ -21,13 +21,17 @@
 //     lane 0 and the east face of the last lane) are computed first, a row a lane.
 //   - Every 16 rows the warp writes the records of the two 16 x 16 groups it covers, with the
 //     reference's 256-slot tree over each group's volumes.
-//   - The last item of a tile to finish commits the tick: the new ledger, the flipped copy and
-//     record buffer, the new largest speeds and the source's clock.
+//   - What a tick writes besides the planes goes to the other of two slots: the tile's first item
+//     writes the new ledger there, and every item adds its largest speeds there by atomicMax. The
+//     last item of a tile to finish flips the copy, the records and the slots, and moves the
+//     source's clock. Nothing a launch writes is read in the same launch, so no item fences its
+//     writes: the next launch sees them at the kernel boundary.
 //
-// Two other shapes share the items, the update (update_cell) and the commit: the split march
-// (tick_split_kernel: a 32 x 16 item by a CTA's four warps, four rows each, for small tiles) and
-// the block tick (tick_block_kernel: a 32 x 16 item by 256 threads in three phases through shared
-// memory; the small-tile default and the stored-faces form). Every shape gives the same bytes.
+// Two other shapes share the items, the update (update_cell) and the last item's flip: the split
+// march (tick_split_kernel: a 32 x 16 item by a CTA's four warps, four rows each, for small tiles)
+// and the block tick (tick_block_kernel: a 32 x 16 item by 256 threads in three phases through
+// shared memory; the small-tile default and the stored-faces form). Every shape gives the same
+// bytes.
 //
 // HBM traffic per cell-update: h, hu, hv, bed read (+ source, + Manning's n, + the remainder when
 // on), h, hu, hv written (+ the remainder), a 32-byte record per 256 cells.
@@ -152,39 +156,31 @@ __device__ void ledger_update(LedgerBits& l, float src, float opn, float rnd, fl
   }
 }
 
-__device__ __forceinline__ void copy_ledger(volatile LedgerBits* dst,
-                                            const volatile LedgerBits* src) {
-  const volatile uint32_t* s = reinterpret_cast<const volatile uint32_t*>(src);
-  volatile uint32_t* d = reinterpret_cast<volatile uint32_t*>(dst);
-#pragma unroll
-  for (int i = 0; i < 12; ++i) d[i] = s[i];
-}
-
-// The end of a work item (one thread, after the item's writes were fenced): its largest speeds
-// into the tile's running maxima and, for the tile's last item, the commit.
-__device__ void finish_item(const TileDesc& T, uint32_t amax, uint32_t bmax, bool tick) {
+// The end of a work item (one thread): its largest speeds into slot rec ^ 1 of the tile's maxima
+// and, for the tile's last item, the flip. No fence: the item's planes, records and maxima are
+// read by the next launch, and the flip reads only fields no other item writes. Every other item
+// of the tile has read slot `rec` (its step's length) before its count, so the last item may clear
+// it. A tick also flips the copy and moves the source's clock; a prime flips only the records.
+__device__ void finish_item(const TileDesc& T, uint32_t rec, uint32_t amax, uint32_t bmax,
+                            bool tick) {
   TileCtl* ctl = T.ctl;
-  atomicMax(&ctl->max_a, amax);
-  atomicMax(&ctl->max_b, bmax);
-  __threadfence();
+  atomicMax(&ctl->max_a[rec ^ 1u], amax);
+  atomicMax(&ctl->max_b[rec ^ 1u], bmax);
   const uint32_t d = atomicAdd(&ctl->done, 1u);
   if (d + 1u != T.items) return;
-  __threadfence();
   volatile TileCtl* v = ctl;
-  v->prev_a = atomicExch(&ctl->max_a, 0u);
-  v->prev_b = atomicExch(&ctl->max_b, 0u);
+  v->max_a[rec] = 0u;
+  v->max_b[rec] = 0u;
   if (tick) {
-    copy_ledger(&v->ledger, &v->ledger_next);
     v->cur = v->cur ^ 1u;
-    v->rec = v->rec ^ 1u;
     if ((T.flags & kFlagSource) != 0u && T.source_every > 1u) {
       const uint32_t p = v->src_phase + 1u;
       v->src_phase = p == T.source_every ? 0u : p;
     }
     v->ticks = v->ticks + 1u;
   }
+  v->rec = rec ^ 1u;
   v->done = 0u;
-  __threadfence();
 }
 
 // ---- the records ----------------------------------------------------------------------------
@@ -216,10 +212,11 @@ __device__ __forceinline__ float group_tree(const float* ring, int gc) {
 // each lane's largest speeds over the group row; the ring holds the volumes of its 16 rows (rows
 // past the grid's edge zero). need_* names the quantities some cell holds. Returns the two groups'
 // largest speeds (lane 0 holds them).
-__device__ __forceinline__ void group_records(const TileDesc& T, Partial* rec_out, int X0,
-                                              int group_row, uint32_t ga, uint32_t gb,
-                                              const float* ring, bool need_src, bool need_opn,
-                                              bool need_rnd, uint32_t& ia, uint32_t& ib) {
+__device__ __forceinline__ void group_records(uint32_t groups_x, uint32_t groups_y,
+                                              Partial* rec_out, int X0, int group_row,
+                                              uint32_t ga, uint32_t gb, const float* ring,
+                                              bool need_src, bool need_opn, bool need_rnd,
+                                              uint32_t& ia, uint32_t& ib) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int o = 8; o > 0; o >>= 1) {
@@ -243,14 +240,14 @@ __device__ __forceinline__ void group_records(const TileDesc& T, Partial* rec_ou
   if (lane == 0) {
     const uint32_t gyg = uint32_t(group_row);
     const uint32_t gx0 = uint32_t(X0 / 16);
-    if (gyg < T.groups_y) {
-      if (gx0 < T.groups_x) {
-        float4* d = reinterpret_cast<float4*>(rec_out + size_t(gyg) * T.groups_x + gx0);
+    if (gyg < groups_y) {
+      if (gx0 < groups_x) {
+        float4* d = reinterpret_cast<float4*>(rec_out + size_t(gyg) * groups_x + gx0);
         d[0] = make_float4(__uint_as_float(ga), __uint_as_float(gb), s0, o0);
         d[1] = make_float4(r0, 0.0f, 0.0f, 0.0f);
       }
-      if (gx0 + 1u < T.groups_x) {
-        float4* d = reinterpret_cast<float4*>(rec_out + size_t(gyg) * T.groups_x + gx0 + 1u);
+      if (gx0 + 1u < groups_x) {
+        float4* d = reinterpret_cast<float4*>(rec_out + size_t(gyg) * groups_x + gx0 + 1u);
         d[0] = make_float4(__uint_as_float(a1), __uint_as_float(b1), s1, o1);
         d[1] = make_float4(r1, 0.0f, 0.0f, 0.0f);
       }
@@ -448,6 +445,9 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   float* qhu = out + n;
   float* qhv = out + 2 * n;
   const float* bed = T.bed;
+  // The planes the rows read, in registers: the march's stores could alias the descriptor.
+  const float* source = T.source;
+  const float* manning_n = T.manning;
   const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
   const float dt = it.dt;
   const uint32_t flags = T.flags;
@@ -471,7 +471,8 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
         gb = max(gb, __float_as_uint(ay));
       }
       if (!SPLIT && ((j & 15) == 15 || j == rows - 1)) {
-        group_records(T, rec_out, X0, gy / 16, ga, gb, ring, false, false, false, ia, ib);
+        group_records(T.groups_x, T.groups_y, rec_out, X0, gy / 16, ga, gb, ring, false, false,
+                      false, ia, ib);
         ga = gb = 0u;
       }
     }
@@ -516,7 +517,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   const int gxc = col ? gx : 0;  // dead lanes read a live column and write nothing
   int i = Y0 * nx + gxc;
   float hu = phu[i], hv = phv[i];
-  float src = it.apply_source ? T.source[i] : 0.0f;
+  float src = it.apply_source ? source[i] : 0.0f;
   float4 c = velocities<FIXED>(ph[i], hu, hv, bed[i], dry);
   float4 fs;
   {
@@ -536,7 +537,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
     nhu = phu[k];
     nhv = phv[k];
     nz = bed[k];
-    if (it.apply_source) nsrc = T.source[k];
+    if (it.apply_source) nsrc = source[k];
   }
 
   const float cell_m = T.cell_m;
@@ -570,7 +571,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
       nhu = phu[k];
       nhv = phv[k];
       nz = bed[k];
-      if (src_on) nsrc = T.source[k];
+      if (src_on) nsrc = source[k];
     }
     const float4 fn = face_y<FIXED>(g, hg, c, nc);
     float4 w = shfl_up4(c);
@@ -584,7 +585,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
     if (col) {
       float h, mu, mv, residual;
       update_cell<FIXED>(uc, c, hu, hv, src, comp ? in[3 * n + i] : 0.0f,
-                         manning ? T.manning[i] : 0.0f, fw, fe, fs, fn, gx, gy, h, mu, mv,
+                         manning ? manning_n[i] : 0.0f, fw, fe, fs, fn, gx, gy, h, mu, mv,
                          residual, csrc, copn, crnd);
       qh[i] = h;
       qhu[i] = mu;
@@ -610,7 +611,8 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
       __syncwarp();
       const bool need_opn = __any_sync(0xffffffffu, opn_seen);
       const bool need_rnd = __any_sync(0xffffffffu, rnd_seen);
-      group_records(T, rec_out, X0, gy / 16, ga, gb, ring, src_on, need_opn, need_rnd, ia, ib);
+      group_records(T.groups_x, T.groups_y, rec_out, X0, gy / 16, ga, gb, ring, src_on, need_opn,
+                    need_rnd, ia, ib);
       ga = gb = 0u;
       opn_seen = rnd_seen = false;
     }
@@ -643,8 +645,9 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
     Item it;
     it.cur = ctl->cur;
     it.rec = ctl->rec;
-    const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
-    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
+    const float pa = __uint_as_float(ctl->max_a[it.rec]);
+    const float pb = __uint_as_float(ctl->max_b[it.rec]);
+    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[it.rec].remaining_s);
     const bool src = (T.flags & kFlagSource) != 0u;
     const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     it.apply_source = on ? 1u : 0u;
@@ -656,18 +659,19 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
       // ring before the march needs it.
       fold_warp(T.rec[it.rec], T.groups_x * T.groups_y, wm.ring);
       if (lane == 0) {
-        LedgerBits l = ctl->ledger;
+        LedgerBits l = ctl->ledger[it.rec];
         ledger_update<FIXED>(l, wm.ring[0], wm.ring[kGroupCells], wm.ring[2 * kGroupCells], pa,
                              pb, T.cfl, T.cell_m, a.max_dt);
-        T.ctl->ledger_next = l;
+        T.ctl->ledger[it.rec ^ 1u] = l;
       }
       __syncwarp();
     }
     uint32_t ia = 0u, ib = 0u;
     march<FIXED, MANNING, H, false>(T, it, wm, wm.ring, 0, nullptr, nullptr, ia, ib);
-    __threadfence();
     __syncwarp();
-    if (lane == 0) finish_item(T, ia, ib, true);
+    // `rec` read again rather than held through the march (a register fewer): only the tile's
+    // last item flips it, after this item's count.
+    if (lane == 0) finish_item(T, T.ctl->rec, ia, ib, true);
     __syncwarp();
   }
   if (lane == 0) {
@@ -708,8 +712,9 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
     Item it;
     it.cur = ctl->cur;
     it.rec = ctl->rec;
-    const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
-    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
+    const float pa = __uint_as_float(ctl->max_a[it.rec]);
+    const float pb = __uint_as_float(ctl->max_b[it.rec]);
+    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[it.rec].remaining_s);
     const bool src = (T.flags & kFlagSource) != 0u;
     const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     it.apply_source = on ? 1u : 0u;
@@ -720,26 +725,23 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
     if (local == 0u && warp == 1) {
       fold_warp(T.rec[it.rec], T.groups_x * T.groups_y, scratch);
       if (lane == 0) {
-        LedgerBits l = ctl->ledger;
+        LedgerBits l = ctl->ledger[it.rec];
         ledger_update<FIXED>(l, scratch[0], scratch[kGroupCells], scratch[2 * kGroupCells], pa,
                              pb, T.cfl, T.cell_m, a.max_dt);
-        T.ctl->ledger_next = l;
+        T.ctl->ledger[it.rec ^ 1u] = l;
       }
       __syncwarp();
     }
     uint32_t ia = 0u, ib = 0u;
     march<FIXED, MANNING, 4, true>(T, it, wm, ring, 4 * warp, s_ab, &s_need, ia, ib);
-    __threadfence();
     __syncthreads();
     if (warp == 0) {
       const uint32_t ga = s_ab[lane < 16 ? 0 : 2], gb = s_ab[lane < 16 ? 1 : 3];
       const uint32_t need = s_need;
-      group_records(T, T.rec[it.rec ^ 1u], it.X0, Y0 / 16, ga, gb, ring,
+      group_records(T.groups_x, T.groups_y, T.rec[it.rec ^ 1u], it.X0, Y0 / 16, ga, gb, ring,
                     it.dt > 0.0f && it.apply_source != 0u, (need & 1u) != 0u, (need & 2u) != 0u,
                     ia, ib);
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) finish_item(T, ia, ib, true);
+      if (lane == 0) finish_item(T, it.rec, ia, ib, true);
     }
     __syncthreads();
   }
@@ -794,20 +796,21 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
     const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
     const TileCtl* ctl = T.ctl;
     const uint32_t cur = ctl->cur, rec = ctl->rec;
-    const float pa = __uint_as_float(ctl->prev_a), pb = __uint_as_float(ctl->prev_b);
-    const float dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger.remaining_s);
+    const float pa = __uint_as_float(ctl->max_a[rec]), pb = __uint_as_float(ctl->max_b[rec]);
+    const float dt =
+        choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[rec].remaining_s);
     const bool src_flag = (T.flags & kFlagSource) != 0u;
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
     const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
     if (local == 0u && warp == 0) {
-      // dt_main's fold of the last update's records (slang:417-478), into the ledger's next copy.
+      // dt_main's fold of the last update's records (slang:417-478), into the ledger's next slot.
       fold_warp(T.rec[rec], T.groups_x * T.groups_y, m.fold);
       if (lane == 0) {
-        LedgerBits l = ctl->ledger;
+        LedgerBits l = ctl->ledger[rec];
         ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
                              T.cfl, T.cell_m, a.max_dt);
-        T.ctl->ledger_next = l;
+        T.ctl->ledger[rec ^ 1u] = l;
       }
       __syncwarp();
     }
@@ -990,17 +993,14 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
     }
     if (lane == 0 && (any_opn || any_rnd))
       atomicOr(&m.need, (any_opn ? 1u : 0u) | (any_rnd ? 2u : 0u));
-    __threadfence();
     __syncthreads();
     if (warp == 0) {
       uint32_t ia = 0u, ib = 0u;
       const uint32_t need = m.need;
-      group_records(T, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[lane < 16 ? 0 : 2],
+      group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[lane < 16 ? 0 : 2],
                     m.ab[lane < 16 ? 1 : 3], m.ring, dt > 0.0f && apply, (need & 1u) != 0u,
                     (need & 2u) != 0u, ia, ib);
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) finish_item(T, ia, ib, true);
+      if (lane == 0) finish_item(T, rec, ia, ib, true);
     }
     __syncthreads();
   }
@@ -1014,7 +1014,9 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
   }
 }
 
-// The records of a state written from the host (prime_main, slang:373-386): a warp an item.
+// The records of a state written from the host (prime_main, slang:373-386): a warp an item. The
+// records and largest speeds go to slot rec ^ 1 and the tile's last item flips `rec`, as a tick
+// does; the tile's first item carries the ledger over to that slot.
 template <bool FIXED, int H>
 __global__ void __launch_bounds__(kCtaThreads) prime_kernel(TickArgs a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1025,6 +1027,8 @@ __global__ void __launch_bounds__(kCtaThreads) prime_kernel(TickArgs a) {
   const TileDesc& T = a.tiles[tile];
   const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
   const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+  const uint32_t rec = T.ctl->rec;
+  if (local == 0u && lane == 0) T.ctl->ledger[rec ^ 1u] = T.ctl->ledger[rec];
   const float* in = T.state[T.ctl->cur];
   const size_t n = size_t(T.nx) * T.ny;
   const int nx = int(T.nx), ny = int(T.ny);
@@ -1042,14 +1046,12 @@ __global__ void __launch_bounds__(kCtaThreads) prime_kernel(TickArgs a) {
       gb = max(gb, __float_as_uint(ay));
     }
     if ((j & 15) == 15 || j == rows - 1) {
-      group_records(T, T.rec[T.ctl->rec], X0, gy / 16, ga, gb, wm.ring, false, false, false, ia,
-                    ib);
+      group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, gy / 16, ga, gb, wm.ring, false,
+                    false, false, ia, ib);
       ga = gb = 0u;
     }
   }
-  __threadfence();
-  __syncwarp();
-  if (lane == 0) finish_item(T, ia, ib, false);
+  if (lane == 0) finish_item(T, rec, ia, ib, false);
 }
 
 // dt_main alone, on one tile (slang:412-479): a flush (max_dt 0) or the length pass. The records'
@@ -1060,13 +1062,14 @@ __global__ void __launch_bounds__(256) length_pass_kernel(const TileDesc* tiles,
   __shared__ float s[3 * kGroupCells];
   __shared__ uint32_t s_ab[2];
   const TileDesc& T = tiles[tile];
-  Partial* rec = T.rec[T.ctl->rec];
+  const uint32_t cr = T.ctl->rec;
+  Partial* rec = T.rec[cr];
   fold_cta(rec, T.groups_x * T.groups_y, s, s_ab);
   if (threadIdx.x == 0) {
-    LedgerBits l = T.ctl->ledger;
+    LedgerBits l = T.ctl->ledger[cr];
     ledger_update<FIXED>(l, s[0], s[kGroupCells], s[2 * kGroupCells], __uint_as_float(s_ab[0]),
                          __uint_as_float(s_ab[1]), T.cfl, T.cell_m, max_dt);
-    T.ctl->ledger = l;
+    T.ctl->ledger[cr] = l;
   }
 }
 
@@ -1075,7 +1078,8 @@ __global__ void __launch_bounds__(256) length_pass_kernel(const TileDesc* tiles,
 __device__ __forceinline__ void reset_ledger(TileCtl* ctl) {
   LedgerBits empty = {};
   empty.remaining_s = __int_as_float(0x7f800000);
-  ctl->ledger = empty;
+  ctl->ledger[0] = empty;
+  ctl->ledger[1] = empty;
   ctl->src_phase = 0u;
 }
 
@@ -1208,13 +1212,14 @@ __global__ void __launch_bounds__(256) flush_all_kernel(const TileDesc* tiles) {
   __shared__ float s[3 * kGroupCells];
   __shared__ uint32_t s_ab[2];
   const TileDesc& T = tiles[blockIdx.x];
-  Partial* rec = T.rec[T.ctl->rec];
+  const uint32_t cr = T.ctl->rec;
+  Partial* rec = T.rec[cr];
   fold_cta(rec, T.groups_x * T.groups_y, s, s_ab);
   if (threadIdx.x == 0) {
-    LedgerBits l = T.ctl->ledger;
+    LedgerBits l = T.ctl->ledger[cr];
     ledger_update<FIXED>(l, s[0], s[kGroupCells], s[2 * kGroupCells], __uint_as_float(s_ab[0]),
                          __uint_as_float(s_ab[1]), T.cfl, T.cell_m, 0.0f);
-    T.ctl->ledger = l;
+    T.ctl->ledger[cr] = l;
   }
 }
 

@@ -43,8 +43,8 @@ __global__ void static_init_kernel(StaticScratch* s, TileDesc d) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   s->desc = d;
   TileCtl c = {};
-  c.ledger.remaining_s = __int_as_float(0x7f800000);
-  c.ledger_next = c.ledger;
+  c.ledger[0].remaining_s = __int_as_float(0x7f800000);
+  c.ledger[1] = c.ledger[0];
   s->ctl = c;
   s->work.next = 0u;
   s->work.exited = 0u;

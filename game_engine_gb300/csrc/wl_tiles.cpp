@@ -212,7 +212,8 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   std::vector<TileCtl> ctl(nt);
   for (TileCtl& c : ctl) {
     std::memset(&c, 0, sizeof c);
-    c.ledger.remaining_s = std::numeric_limits<float>::infinity();
+    c.ledger[0].remaining_s = std::numeric_limits<float>::infinity();
+    c.ledger[1].remaining_s = std::numeric_limits<float>::infinity();
   }
   if (!check(cudaMemcpyAsync(d_ctl_, ctl.data(), nt * sizeof(TileCtl), cudaMemcpyHostToDevice,
                              stream_),
@@ -453,10 +454,12 @@ bool TileSet::set_flags(uint32_t tile, uint32_t flags, uint32_t source_every, bo
 
 bool TileSet::set_remaining(uint32_t tile, float remaining, std::string* err) {
   if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
-  if (!check(cudaMemcpyAsync(&d_ctl_[tile].ledger.remaining_s, &remaining, sizeof remaining,
-                             cudaMemcpyHostToDevice, stream_),
-             err, "upload of the time left"))
-    return false;
+  // Both slots: the current one is read by the next tick, the other is rewritten from it.
+  for (int k = 0; k < 2; ++k)
+    if (!check(cudaMemcpyAsync(&d_ctl_[tile].ledger[k].remaining_s, &remaining, sizeof remaining,
+                               cudaMemcpyHostToDevice, stream_),
+               err, "upload of the time left"))
+      return false;
   return wait(err);
 }
 
