@@ -66,6 +66,25 @@ class Tuning(C.Structure):
     _fields_ = [("block_rows", C.c_uint32), ("order", C.c_uint32), ("us_per_tick", C.c_float)]
 
 
+class Event(C.Structure):
+    """wl_event: a rectangle of one plane a queued tick replaces."""
+    _fields_ = [("kind", C.c_uint32), ("x0", C.c_uint32), ("y0", C.c_uint32), ("w", C.c_uint32),
+                ("h", C.c_uint32)]
+
+
+class Landed(C.Structure):
+    """wl_landed: a landed tick's read-back record."""
+    _fields_ = [("tick", C.c_uint32), ("substeps", C.c_uint32), ("shortest_s", C.c_float),
+                ("longest_s", C.c_float), ("time_hi", C.c_float), ("time_lo", C.c_float),
+                ("steps", C.c_uint32), ("events", C.c_uint32)]
+
+
+class QueueStatus(C.Structure):
+    """wl_queue_status: the queue's counts."""
+    _fields_ = [("pushed", C.c_uint32), ("begun", C.c_uint32), ("landed", C.c_uint32),
+                ("active", C.c_uint32), ("substeps", C.c_uint32), ("pad", C.c_uint32 * 3)]
+
+
 _u64p = C.POINTER(C.c_uint64)
 _u32p = C.POINTER(C.c_uint32)
 
@@ -134,6 +153,19 @@ SIGNATURES = {
     # one tick that allocates nothing
     "wl_tick_noalloc": (C.c_int, [C.POINTER(Config), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_float, wl_stream, *_err]),
+    # the tick queue
+    "wl_queue_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                  C.POINTER(C.c_void_p), *_err]),
+    "wl_queue_destroy": (None, [C.c_void_p]),
+    "wl_queue_push": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.POINTER(Event), C.c_uint32,
+                                _fp, C.c_size_t, *_err]),
+    "wl_queue_enqueue_slots": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32]),
+    "wl_queue_run_slots": (C.c_int, [C.c_void_p, C.c_uint32, *_err]),
+    "wl_queue_status_read": (C.c_int, [C.c_void_p, C.POINTER(QueueStatus), *_err]),
+    "wl_queue_read_landed": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(Landed),
+                                       *_err]),
+    "wl_queue_launches_per_slot": (C.c_uint32, []),
+    "wl_queue_device_bytes": (C.c_uint64, [C.c_void_p]),
 }
 
 

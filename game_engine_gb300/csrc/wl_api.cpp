@@ -3,6 +3,7 @@
 #include "wlcuda.h"
 
 #include "wl_adjoint.h"
+#include "wl_queue.h"
 #include "wl_tiles.h"
 
 #include <cstddef>
@@ -23,6 +24,12 @@ struct wl_step {
   uint32_t source_every = 1;
   uint32_t cells = 0;
   uint32_t groups = 0;
+  wl_queue* queue = nullptr;  // the tick queue attached, which owns the step's clock
+};
+
+struct wl_queue {
+  wl_step* step = nullptr;  // null once the step was destroyed
+  wlc::TickQueue q;
 };
 
 // The mirrored structs keep the reference's sizes and offsets (water_live_tests.cpp:22-36,
@@ -62,6 +69,7 @@ int cuda_fail(char* err, size_t len, const std::string& msg) {
 bool valid(const wl_step* s) { return s != nullptr && s->set.valid(); }
 
 const char* k_no_device = "water_live: no device";
+const char* k_queued = "water_live: the step's tick queue owns its clock (destroy the queue first)";
 
 int flush(wl_step* s, wl_ledger_bits* bits, std::string* msg) {
   if (!s->set.length_pass(0, 0.0f, msg)) return WL_ERR_CUDA;
@@ -142,7 +150,13 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
   return WL_OK;
 }
 
-void wl_destroy(wl_step* step) { delete step; }
+void wl_destroy(wl_step* step) {
+  if (step != nullptr && step->queue != nullptr) {
+    step->queue->q.destroy();
+    step->queue->step = nullptr;
+  }
+  delete step;
+}
 
 int wl_valid(const wl_step* step) { return valid(step) ? 1 : 0; }
 
@@ -153,6 +167,8 @@ uint32_t wl_group_count(const wl_step* step) { return valid(step) ? step->groups
 int wl_write_state(wl_step* s, const double* h, const double* hu, const double* hv, size_t n,
                    char* err, size_t err_len) {
   if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  // A new state empties the ledger, time left included: the queue's tick in flight could not land.
+  if (s->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (n != s->cells || h == nullptr || hu == nullptr || hv == nullptr)
     return fail(err, err_len, WL_ERR_SIZE, "water_live: a state that does not fit the grid");
   std::string msg;
@@ -220,6 +236,10 @@ int wl_set_manning(wl_step* s, const double* manning, size_t n, char* err, size_
 int wl_set_source(wl_step* s, const double* source, size_t n, uint32_t every, int compensate,
                   char* err, size_t err_len) {
   if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  // A coarser source clock cannot follow the sub-steps a queue's card chooses (water_live.md:92).
+  if (s->queue != nullptr && every > 1)
+    return fail(err, err_len, WL_ERR_REFUSED,
+                "water_live: a step with a tick queue refuses a coarser source clock");
   // water_live.cpp:465-486: the clock and the compensation change even when the source is refused.
   s->source_every = every == 0 ? 1 : every;
   if (compensate) s->flags |= WL_FLAG_COMPENSATE;
@@ -245,6 +265,7 @@ int wl_set_source(wl_step* s, const double* source, size_t n, uint32_t every, in
 
 int wl_enqueue_steps(wl_step* s, wl_stream stream, uint32_t count, float max_dt) {
   if (!valid(s)) return WL_ERR_INVALID;
+  if (s->queue != nullptr) return WL_ERR_REFUSED;
   cudaStream_t st = stream == nullptr ? s->set.stream() : reinterpret_cast<cudaStream_t>(stream);
   if (cudaSetDevice(s->set.device()) != cudaSuccess) return WL_ERR_CUDA;
   return s->set.enqueue_ticks(st, count, max_dt) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
@@ -252,6 +273,7 @@ int wl_enqueue_steps(wl_step* s, wl_stream stream, uint32_t count, float max_dt)
 
 int wl_run_steps(wl_step* s, uint32_t count, float max_dt, char* err, size_t err_len) {
   if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (s->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (cudaSetDevice(s->set.device()) != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
   const cudaError_t e = s->set.enqueue_ticks(s->set.stream(), count, max_dt);
@@ -268,6 +290,10 @@ uint64_t wl_advance(wl_step* s, double duration_s, char* err, size_t err_len) {
     return 0;
   }
   if (!(duration_s > 0.0)) return 0;
+  if (s->queue != nullptr) {
+    fail(err, err_len, WL_ERR_REFUSED, k_queued);
+    return 0;
+  }
   // water_live.cpp:600-606: a coarser source clock counts steps on the host; refused.
   if ((s->flags & WL_FLAG_SOURCE) != 0u && s->source_every > 1) {
     fail(err, err_len, WL_ERR_REFUSED,
@@ -359,6 +385,7 @@ wl_stream wl_step_stream(wl_step* s) {
 
 int wl_write_state_device(wl_step* s, const float* planes, wl_stream stream) {
   if (!valid(s)) return WL_ERR_INVALID;
+  if (s->queue != nullptr) return WL_ERR_REFUSED;
   if (planes == nullptr) return WL_ERR_ARGUMENT;
   if (cudaSetDevice(s->set.device()) != cudaSuccess) return WL_ERR_CUDA;
   cudaStream_t st = stream == nullptr ? s->set.stream() : reinterpret_cast<cudaStream_t>(stream);
@@ -388,6 +415,107 @@ int wl_adjoint_create(wl_step* step, uint32_t ticks, uint32_t every, uint32_t n_
   const uint32_t first[2] = {0u, n_probes};
   return wl_adjoint_create_over(&step->set, ticks, every, first, probes, targets, out, err,
                                 err_len);
+}
+
+// ---- the tick queue (water_live.md:76-94) -----------------------------------------------------
+
+int wl_queue_create(wl_step* step, uint32_t records, uint32_t arena_values, uint32_t max_events,
+                    wl_queue** out, char* err, size_t err_len) {
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no handle to fill");
+  *out = nullptr;
+  if (!valid(step)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (step->queue != nullptr)
+    return fail(err, err_len, WL_ERR_REFUSED, "water_live: the step has a tick queue already");
+  if ((step->flags & WL_FLAG_SOURCE) != 0u && step->source_every > 1)
+    return fail(err, err_len, WL_ERR_REFUSED,
+                "water_live: a tick queue refuses a source on a coarser clock (set_source every > 1)");
+  auto* q = new (std::nothrow) wl_queue;
+  if (q == nullptr) return fail(err, err_len, WL_ERR_ALLOC, "water_live: host memory");
+  std::string msg;
+  if (!q->q.create(&step->set, records, arena_values, max_events, &msg)) {
+    delete q;
+    const int code = msg.find("holds 1 to 64") != std::string::npos ? WL_ERR_ARGUMENT : WL_ERR_CUDA;
+    return fail(err, err_len, code, msg);
+  }
+  q->step = step;
+  step->queue = q;
+  *out = q;
+  return WL_OK;
+}
+
+void wl_queue_destroy(wl_queue* queue) {
+  if (queue == nullptr) return;
+  if (queue->step != nullptr) {
+    queue->q.destroy();
+    queue->step->queue = nullptr;
+  }
+  delete queue;
+}
+
+int wl_queue_push(wl_queue* queue, uint32_t tick, float length_s, const wl_event* events,
+                  uint32_t n_events, const float* values, size_t n_values, char* err,
+                  size_t err_len) {
+  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+    return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
+  std::string msg;
+  const int rc = queue->q.push(tick, length_s, events, n_events, values, n_values, &msg);
+  return rc == WL_OK ? WL_OK : fail(err, err_len, rc, msg);
+}
+
+int wl_queue_enqueue_slots(wl_queue* queue, wl_stream stream, uint32_t slots) {
+  if (queue == nullptr || queue->step == nullptr || !queue->q.valid()) return WL_ERR_INVALID;
+  wl_step* s = queue->step;
+  cudaStream_t st = stream == nullptr ? s->set.stream() : reinterpret_cast<cudaStream_t>(stream);
+  if (cudaSetDevice(s->set.device()) != cudaSuccess) return WL_ERR_CUDA;
+  return queue->q.enqueue(st, slots) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
+}
+
+int wl_queue_run_slots(wl_queue* queue, uint32_t slots, char* err, size_t err_len) {
+  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+    return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
+  wl_step* s = queue->step;
+  if (cudaSetDevice(s->set.device()) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
+  const cudaError_t e = queue->q.enqueue(s->set.stream(), slots);
+  if (e != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, std::string("water_live: the slots: ") + cudaGetErrorString(e));
+  std::string msg;
+  if (!s->set.wait(&msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
+int wl_queue_status_read(wl_queue* queue, wl_queue_status* out, char* err, size_t err_len) {
+  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+    return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no status to fill");
+  wlc::QueueCtl c;
+  std::string msg;
+  if (!queue->q.read_ctl(c, &msg)) return cuda_fail(err, err_len, msg);
+  std::memset(out, 0, sizeof *out);
+  out->pushed = c.head;
+  out->begun = c.begun;
+  out->landed = c.landed;
+  out->active = c.active;
+  out->substeps = c.substeps;
+  return WL_OK;
+}
+
+int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_landed* out,
+                         char* err, size_t err_len) {
+  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+    return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
+  std::string msg;
+  if (!queue->q.read_landed(first, count, out, &msg)) {
+    const int code = msg.find("not held") != std::string::npos ? WL_ERR_ARGUMENT : WL_ERR_CUDA;
+    return fail(err, err_len, code, msg);
+  }
+  return WL_OK;
+}
+
+uint32_t wl_queue_launches_per_slot(void) { return 3u; }
+
+uint64_t wl_queue_device_bytes(const wl_queue* queue) {
+  return queue != nullptr && queue->step != nullptr ? queue->q.device_bytes() : 0u;
 }
 
 }  // extern "C"

@@ -630,6 +630,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
 // The persistent tick: every work item of every tile, one tick.
 template <bool FIXED, bool MANNING, int H>
 __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
+  if (a.go != nullptr && *a.go == 0u) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const WarpMem<H> wm = warp_mem<H>(warp);
   for (;;) {
@@ -689,6 +690,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
 // The items are the 32 x 16 shape's.
 template <bool FIXED, bool MANNING>
 __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) {
+  if (a.go != nullptr && *a.go == 0u) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const WarpMem<4> wm = warp_mem<4>(warp);
   float* ring = warp_mem<4>(0).ring;     // the item's 16 rows of volumes
@@ -778,6 +780,7 @@ struct BlockSmem {
 
 template <bool FIXED, bool MANNING>
 __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) {
+  if (a.go != nullptr && *a.go == 0u) return;
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;

@@ -11,13 +11,15 @@ struct TileDesc;
 struct WorkCtl;
 
 // A tick launch: the tiles, which tile each work item belongs to (null: all items of tile 0), the
-// launch's work counter and the step's max_dt.
+// launch's work counter and the step's max_dt. `go`, when not null, is a device word read at the
+// start: zero makes the launch return before it takes any item (a tick queue's idle slot).
 struct TickArgs {
   const TileDesc* tiles;
   const uint32_t* item_tile;
   WorkCtl* work;
   uint32_t n_items;
   float max_dt;
+  const uint32_t* go = nullptr;
 };
 
 // The block of cells one work item steps: 32 columns by 16, 32 or 64 rows, one warp marching

@@ -1,0 +1,336 @@
+// The tick queue's kernels and host side (wl_queue.h). A slot is three launches on one stream:
+//
+//   queue_begin_kernel  one thread: settles the last slot (counts its sub-step, lands a tick whose
+//                       time left reached zero, releases the events the last apply read), then,
+//                       when no tick is in flight and one is queued, begins it by setting the
+//                       step's time left to its length; writes the slot's `go` and `apply` words.
+//   queue_apply_kernel  one CTA: the begun tick's events into the step's planes, in push order.
+//   the tick            the step's own persistent tick (wl_kernels.cu) with max_dt = +inf, so a
+//                       sub-step is min(stable step, time left); it returns at once when `go` is 0.
+//
+// The time left is the reference's ledger field (WaterLedger::remaining_s, water_live.h:124-137)
+// that its advance counts down (water_live.cpp:590-639), so a queued tick takes the sub-steps
+// wl_advance takes for the same length. The begun tick's events write the planes before its first
+// sub-step and after the last sub-step of the tick before: the tick's own boundary
+// (water_live.md:86). A bed, source or Manning plane enters no record (the records hold the
+// state's speeds and volumes), so an event needs no prime.
+#include "wl_kernels.h"
+#include "wl_queue.h"
+
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+namespace wlc {
+namespace {
+
+constexpr uint32_t kMaxRecords = 64;  // water_live.md:84
+constexpr int kApplyThreads = 1024;
+
+// The tick in flight's read-back record, and the queue free for the next.
+__device__ void land(QueueCtl* q, const LedgerBits& l, wl_landed* landed, uint32_t records) {
+  wl_landed r;
+  r.tick = q->tick;
+  r.substeps = q->substeps;
+  r.shortest_s = q->substeps != 0u ? q->shortest : 0.0f;
+  r.longest_s = q->longest;
+  r.time_hi = l.time_hi;
+  r.time_lo = l.time_lo;
+  r.steps = l.steps;
+  r.events = q->events;
+  landed[q->landed % records] = r;
+  q->landed += 1u;
+  q->active = 0u;
+}
+
+// The last slot's effects: the release of the events its apply read, its sub-step (the ledger's
+// step count moved) and a landing (a tick in flight with no time left).
+__device__ void settle(QueueCtl* q, const TileCtl* ctl, wl_landed* landed, uint32_t records) {
+  const LedgerBits& l = ctl->ledger[ctl->rec];
+  if (q->apply != 0u) {
+    q->events_done = q->first_event + q->events;
+    q->values_done = q->values_end;
+    q->apply = 0u;
+  }
+  if (l.steps != q->seen_steps) {
+    q->seen_steps = l.steps;
+    q->substeps += 1u;
+    q->shortest = fminf(q->shortest, l.dt);
+    q->longest = fmaxf(q->longest, l.dt);
+  }
+  if (q->active != 0u && !(l.remaining_s > 0.0f)) land(q, l, landed, records);
+}
+
+__global__ void queue_begin_kernel(QueueCtl* q, const QueueRecord* ring, TileCtl* ctl,
+                                   wl_landed* landed, uint32_t records, int may_begin) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  volatile QueueCtl* vq = q;
+  settle(q, ctl, landed, records);
+  const uint32_t head = vq->head;  // the host's word
+  if (may_begin != 0 && q->active == 0u && q->begun != head) {
+    const QueueRecord r = ring[q->begun % records];
+    q->begun += 1u;
+    q->tick = r.tick;
+    q->events = r.events;
+    q->first_event = r.first_event;
+    q->values_end = r.values_end;
+    q->substeps = 0u;
+    q->shortest = __int_as_float(0x7f800000);
+    q->longest = 0.0f;
+    q->apply = r.events != 0u ? 1u : 0u;
+    q->active = 1u;
+    LedgerBits& l = ctl->ledger[ctl->rec];
+    l.remaining_s = r.length_s > 0.0f ? r.length_s : 0.0f;
+    // A tick of no length lands now; its events are applied later in this slot all the same.
+    if (!(r.length_s > 0.0f)) land(q, l, landed, records);
+  }
+  q->go = q->active;
+}
+
+// The begun tick's events, one after another (a later event over the same cells wins). The host
+// checked every rectangle against the grid and every plane's presence when it pushed them.
+__global__ void __launch_bounds__(kApplyThreads) queue_apply_kernel(const QueueCtl* q,
+                                                                    const QueueEvent* events,
+                                                                    uint32_t max_events,
+                                                                    const float* arena,
+                                                                    uint32_t arena_values,
+                                                                    const TileDesc* T) {
+  if (q->apply == 0u) return;
+  const uint32_t n = q->events;
+  const uint64_t first = q->first_event;
+  for (uint32_t e = 0; e < n; ++e) {
+    const QueueEvent ev = events[(first + e) % max_events];
+    float* dst = const_cast<float*>(ev.kind == WL_EVENT_BED      ? T->bed
+                                    : ev.kind == WL_EVENT_SOURCE ? T->source
+                                                                 : T->manning);
+    const float* src = arena + ev.value_first % arena_values;
+    const uint32_t count = ev.w * ev.h;
+    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
+      const uint32_t y = k / ev.w, x = k - y * ev.w;
+      dst[size_t(ev.y0 + y) * T->nx + ev.x0 + x] = src[k];
+    }
+    __syncthreads();
+  }
+}
+
+size_t align_up(size_t v) { return (v + 255) & ~size_t(255); }
+
+bool ok(cudaError_t e, std::string* err, const char* what) {
+  if (e == cudaSuccess) return true;
+  if (err) *err = std::string("water_live: ") + what + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+}  // namespace
+
+bool TickQueue::create(TileSet* set, uint32_t records, uint32_t arena_values, uint32_t max_events,
+                       std::string* err) {
+  destroy();
+  if (set == nullptr || !set->valid()) {
+    if (err) *err = "water_live: no step";
+    return false;
+  }
+  if (records == 0 || records > kMaxRecords || max_events == 0 || arena_values == 0) {
+    if (err) *err = "water_live: a queue holds 1 to 64 records, and at least one event and value";
+    return false;
+  }
+  if (!ok(cudaSetDevice(set->device()), err, "cudaSetDevice")) return false;
+  const size_t b_ctl = align_up(sizeof(QueueCtl));
+  const size_t b_ring = align_up(size_t(records) * sizeof(QueueRecord));
+  const size_t b_events = align_up(size_t(max_events) * sizeof(QueueEvent));
+  const size_t b_landed = align_up(size_t(records) * sizeof(wl_landed));
+  const size_t b_arena = align_up(size_t(arena_values) * sizeof(float));
+  bytes_ = b_ctl + b_ring + b_events + b_landed + b_arena;
+  if (!ok(cudaMalloc(reinterpret_cast<void**>(&base_), bytes_), err, "cudaMalloc of the queue")) {
+    base_ = nullptr;
+    return false;
+  }
+  d_ctl_ = reinterpret_cast<QueueCtl*>(base_);
+  d_ring_ = reinterpret_cast<QueueRecord*>(base_ + b_ctl);
+  d_events_ = reinterpret_cast<QueueEvent*>(base_ + b_ctl + b_ring);
+  d_landed_ = reinterpret_cast<wl_landed*>(base_ + b_ctl + b_ring + b_events);
+  d_arena_ = reinterpret_cast<float*>(base_ + b_ctl + b_ring + b_events + b_landed);
+  set_ = set;
+  records_ = records;
+  max_events_ = max_events;
+  arena_ = arena_values;
+  pushed_ = 0;
+  events_pushed_ = 0;
+  values_pushed_ = 0;
+  // The settle counts sub-steps from the ledger's step count as it stands now.
+  TileCtl c;
+  if (!set->read_ctl(0, c, err)) {
+    destroy();
+    return false;
+  }
+  QueueCtl q;
+  std::memset(&q, 0, sizeof q);
+  q.seen_steps = c.ledger[c.rec & 1u].steps;
+  if (!ok(cudaMemsetAsync(base_, 0, bytes_, set->stream()), err, "cudaMemset of the queue") ||
+      !ok(cudaMemcpyAsync(d_ctl_, &q, sizeof q, cudaMemcpyHostToDevice, set->stream()), err,
+          "upload of the queue") ||
+      !set->wait(err)) {
+    destroy();
+    return false;
+  }
+  return true;
+}
+
+void TickQueue::destroy() {
+  if (base_ != nullptr) {
+    if (set_ != nullptr && set_->valid()) {
+      cudaSetDevice(set_->device());
+      cudaStreamSynchronize(set_->stream());
+      // The step's clock back to the free-running form: no time to count down.
+      std::string ignored;
+      set_->set_remaining(0, std::numeric_limits<float>::infinity(), &ignored);
+    }
+    cudaFree(base_);
+  }
+  base_ = nullptr;
+  set_ = nullptr;
+  bytes_ = 0;
+}
+
+bool TickQueue::read_ctl(QueueCtl& out, std::string* err) {
+  if (!valid()) {
+    if (err) *err = "water_live: no queue";
+    return false;
+  }
+  if (!ok(cudaSetDevice(set_->device()), err, "cudaSetDevice") ||
+      !ok(cudaMemcpyAsync(&out, d_ctl_, sizeof out, cudaMemcpyDeviceToHost, set_->stream()), err,
+          "read-back of the queue"))
+    return false;
+  return set_->wait(err);
+}
+
+int TickQueue::push(uint32_t tick, float length_s, const wl_event* events, uint32_t n_events,
+                    const float* values, size_t n_values, std::string* err) {
+  if (!valid()) {
+    if (err) *err = "water_live: no queue";
+    return WL_ERR_INVALID;
+  }
+  if (!(length_s >= 0.0f) || length_s == std::numeric_limits<float>::infinity()) {
+    if (err) *err = "water_live: a tick's length is finite and not negative";
+    return WL_ERR_ARGUMENT;
+  }
+  if (n_events > 0 && events == nullptr) {
+    if (err) *err = "water_live: no events";
+    return WL_ERR_ARGUMENT;
+  }
+  const TileDesc& d = set_->desc(0);
+  uint64_t need = 0;
+  for (uint32_t e = 0; e < n_events; ++e) {
+    const wl_event& ev = events[e];
+    const bool plane = ev.kind == WL_EVENT_BED ||
+                       (ev.kind == WL_EVENT_SOURCE && d.source != nullptr &&
+                        (d.flags & kFlagSource) != 0u) ||
+                       (ev.kind == WL_EVENT_MANNING && d.manning != nullptr &&
+                        (d.flags & kFlagManning) != 0u);
+    if (!plane) {
+      if (err) *err = "water_live: an event's plane is not on (set the source or Manning's n first)";
+      return WL_ERR_ARGUMENT;
+    }
+    if (ev.w == 0 || ev.h == 0 || uint64_t(ev.x0) + ev.w > d.nx || uint64_t(ev.y0) + ev.h > d.ny) {
+      if (err) *err = "water_live: an event's rectangle is empty or leaves the grid";
+      return WL_ERR_SIZE;
+    }
+    need += uint64_t(ev.w) * ev.h;
+  }
+  if (need != n_values || (need > 0 && values == nullptr)) {
+    if (err) *err = "water_live: the values do not match the events' rectangles";
+    return WL_ERR_SIZE;
+  }
+  if (need > arena_ || n_events > max_events_) {
+    if (err) *err = "water_live: the tick's events are larger than the queue's arena or event ring";
+    return WL_ERR_SIZE;
+  }
+  QueueCtl q;
+  if (!read_ctl(q, err)) return WL_ERR_CUDA;
+  // A push is whole in the arena: values that would run past its end start again at 0.
+  uint64_t base = values_pushed_;
+  if (base % arena_ + need > arena_) base += arena_ - base % arena_;
+  const bool room = pushed_ - q.begun < records_ &&
+                    events_pushed_ + n_events - q.events_done <= max_events_ &&
+                    base + need - q.values_done <= arena_;
+  if (!room) {
+    if (err) *err = "water_live: the queue has no room yet";
+    return WL_ERR_REFUSED;
+  }
+  cudaStream_t s = set_->stream();
+  std::vector<QueueEvent> dev(n_events);
+  uint64_t at = base;
+  for (uint32_t e = 0; e < n_events; ++e) {
+    const wl_event& ev = events[e];
+    dev[e] = QueueEvent{ev.kind, ev.x0, ev.y0, ev.w, ev.h, 0u, at};
+    at += uint64_t(ev.w) * ev.h;
+  }
+  // Events and values first, the record, then `head`: a slot that sees the new head finds them.
+  for (uint32_t e = 0; e < n_events; ++e) {
+    const uint64_t slot = (events_pushed_ + e) % max_events_;
+    if (!ok(cudaMemcpyAsync(d_events_ + slot, &dev[e], sizeof(QueueEvent), cudaMemcpyHostToDevice,
+                            s),
+            err, "upload of an event"))
+      return WL_ERR_CUDA;
+  }
+  if (need > 0 && !ok(cudaMemcpyAsync(d_arena_ + base % arena_, values, need * sizeof(float),
+                                      cudaMemcpyHostToDevice, s),
+                      err, "upload of the events' values"))
+    return WL_ERR_CUDA;
+  // A record releases the arena up to its own values' end; one with none, up to the values
+  // pushed before it (all of them released by then, records being begun in order).
+  const uint64_t values_end = need > 0 ? base + need : values_pushed_;
+  QueueRecord r{tick, length_s, events_pushed_, n_events, 0u, values_end};
+  const uint32_t head = pushed_ + 1u;
+  if (!ok(cudaMemcpyAsync(d_ring_ + pushed_ % records_, &r, sizeof r, cudaMemcpyHostToDevice, s),
+          err, "upload of a record") ||
+      !ok(cudaMemcpyAsync(&d_ctl_->head, &head, sizeof head, cudaMemcpyHostToDevice, s), err,
+          "upload of the queue's head") ||
+      !set_->wait(err))
+    return WL_ERR_CUDA;
+  pushed_ = head;
+  events_pushed_ += n_events;
+  if (need > 0) values_pushed_ = base + need;
+  return WL_OK;
+}
+
+cudaError_t TickQueue::enqueue(cudaStream_t s, uint32_t slots) {
+  if (!valid()) return cudaErrorInvalidValue;
+  const TileDesc& d = set_->desc(0);
+  const float inf = std::numeric_limits<float>::infinity();
+  for (uint32_t k = 0; k < slots; ++k) {
+    queue_begin_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    queue_apply_kernel<<<1, kApplyThreads, 0, s>>>(d_ctl_, d_events_, max_events_, d_arena_,
+                                                    arena_, set_->device_descs());
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = set_->enqueue_ticks(s, 1, inf, &d_ctl_->go);
+    if (e != cudaSuccess) return e;
+  }
+  // The last slot's effects, so a read-back after the call sees them.
+  queue_begin_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 0);
+  return cudaGetLastError();
+}
+
+bool TickQueue::read_landed(uint32_t first, uint32_t count, wl_landed* out, std::string* err) {
+  QueueCtl q;
+  if (!read_ctl(q, err)) return false;
+  if (count == 0) return true;
+  if (out == nullptr || uint64_t(first) + count > q.landed || q.landed - first > records_) {
+    if (err) *err = "water_live: those landings are not held (the last `records` are)";
+    return false;
+  }
+  std::vector<wl_landed> all(records_);
+  if (!ok(cudaMemcpyAsync(all.data(), d_landed_, records_ * sizeof(wl_landed),
+                          cudaMemcpyDeviceToHost, set_->stream()),
+          err, "read-back of the landings") ||
+      !set_->wait(err))
+    return false;
+  for (uint32_t i = 0; i < count; ++i) out[i] = all[(first + i) % records_];
+  return true;
+}
+
+}  // namespace wlc

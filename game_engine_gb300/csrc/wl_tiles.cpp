@@ -315,13 +315,15 @@ bool TileSet::push_desc(uint32_t tile, std::string* err) {
   return check(cudaStreamSynchronize(stream_), err, "cudaStreamSynchronize");
 }
 
-cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt) {
+cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
+                                   const uint32_t* go) {
   TickArgs a;
   a.tiles = d_desc_;
   a.item_tile = d_item_tile_;
   a.work = d_work_;
   a.n_items = n_items_;
   a.max_dt = max_dt;
+  a.go = go;
   const bool manning = any_manning();
   for (uint32_t i = 0; i < count; ++i) {
     const cudaError_t e = launch_tick(shape_, fixed_, manning, a, grid_, s);

@@ -39,7 +39,9 @@ class TileSet {
   bool reshape(BlockShape shape, const std::vector<uint32_t>& order, std::string* err);
 
   // ---- asynchronous, on `s` -----------------------------------------------------------------
-  cudaError_t enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt);
+  // `go`: a tick queue's word that lets the launches step (null: always).
+  cudaError_t enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
+                            const uint32_t* go = nullptr);
   // One tile's own tick (the per-tile-launch form): only that tile's work items.
   cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);
   cudaError_t enqueue_prime(cudaStream_t s);

@@ -1,0 +1,118 @@
+"""The tick queue over the C ABI (include/wlcuda.h, "the tick queue").
+
+The design is the reference's (docs/subsystems/water_live.md:76-94, ADR-0081), which the reference
+has not built: ticks of the world's clock, each a length and the events that take effect at its
+start, queued on the device and stepped by sub-step slots. Calls that move data return
+``True``/``False`` and leave the message in :attr:`TickQueue.error`, as ``DeviceStep`` does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi, lib
+
+EVENT_BED, EVENT_SOURCE, EVENT_MANNING = 0, 1, 2
+ERR_REFUSED = 5
+MAX_RECORDS = 64
+
+_fp = C.POINTER(C.c_float)
+
+
+@dataclass
+class Event:
+    """A rectangle of one plane (EVENT_*) replaced by ``values`` (h rows of w, row by row)."""
+    kind: int
+    x0: int
+    y0: int
+    values: np.ndarray  # shape (h, w)
+
+
+class TickQueue:
+    """The queue of ticks over one ``water_live.DeviceStep``."""
+
+    def __init__(self, step, records: int = MAX_RECORDS, arena_values: int = 1 << 16,
+                 max_events: int = 256):
+        self.error = ""
+        self.last_code = 0
+        self._buf = C.create_string_buffer(512)
+        self._h = None
+        self._step = step
+        h = C.c_void_p()
+        rc = lib().wl_queue_create(step.handle, int(records), int(arena_values), int(max_events),
+                                   C.byref(h), self._buf, len(self._buf))
+        if rc != 0:
+            raise RuntimeError(self._buf.value.decode())
+        self._h = h
+
+    def close(self) -> None:
+        if self._h is not None:
+            lib().wl_queue_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc: int) -> bool:
+        self.last_code = rc
+        if rc != 0:
+            self.error = self._buf.value.decode()
+            return False
+        return True
+
+    def push(self, tick: int, length_s: float, events=()) -> bool:
+        """Queues one tick; False with ``last_code`` ERR_REFUSED when the queue has no room yet."""
+        evs = (_abi.Event * max(len(events), 1))()
+        vals = []
+        for k, e in enumerate(events):
+            v = np.ascontiguousarray(e.values, dtype=np.float32)
+            h, w = v.shape
+            evs[k] = _abi.Event(int(e.kind), int(e.x0), int(e.y0), int(w), int(h))
+            vals.append(v.ravel())
+        flat = np.concatenate(vals) if vals else np.zeros(1, np.float32)
+        n_values = int(sum(v.size for v in vals))
+        return self._ok(lib().wl_queue_push(self._h, int(tick) & 0xFFFFFFFF, float(length_s), evs,
+                                            len(events), flat.ctypes.data_as(_fp), n_values,
+                                            self._buf, len(self._buf)))
+
+    def enqueue_slots(self, stream, slots: int) -> bool:
+        """``slots`` slots on a CUDA stream (an int handle, or None for the step's own); no wait."""
+        rc = lib().wl_queue_enqueue_slots(self._h, stream, int(slots))
+        if rc != 0:
+            self.error = f"water_live: enqueue of the slots failed ({rc})"
+            self.last_code = rc
+            return False
+        return True
+
+    def run_slots(self, slots: int) -> bool:
+        return self._ok(lib().wl_queue_run_slots(self._h, int(slots), self._buf, len(self._buf)))
+
+    def status(self):
+        s = _abi.QueueStatus()
+        if not self._ok(lib().wl_queue_status_read(self._h, C.byref(s), self._buf,
+                                                   len(self._buf))):
+            return None
+        return dict(pushed=s.pushed, begun=s.begun, landed=s.landed, active=s.active,
+                    substeps=s.substeps)
+
+    def landed(self, first: int, count: int):
+        """The read-back records of landings first .. first + count - 1, as dicts."""
+        out = (_abi.Landed * max(count, 1))()
+        if not self._ok(lib().wl_queue_read_landed(self._h, int(first), int(count), out,
+                                                   self._buf, len(self._buf))):
+            return None
+        return [dict(tick=r.tick, substeps=r.substeps, shortest_s=r.shortest_s,
+                     longest_s=r.longest_s, time_hi=r.time_hi, time_lo=r.time_lo, steps=r.steps,
+                     events=r.events) for r in out[:count]]
+
+    @staticmethod
+    def launches_per_slot() -> int:
+        return int(lib().wl_queue_launches_per_slot())
+
+    def device_bytes(self) -> int:
+        return int(lib().wl_queue_device_bytes(self._h)) if self._h is not None else 0

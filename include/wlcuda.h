@@ -309,6 +309,84 @@ int wl_tick_noalloc(const wl_config* config, int fixed_ops, const float* planes_
                     const float* source, float max_dt, wl_stream stream, char* err,
                     size_t err_len);
 
+/* ---- the tick queue (designed in docs/subsystems/water_live.md:76-94, ADR-0081; the reference
+ * builds none of it) ----------------------------------------------------------------------------
+ *
+ * Ticks of the world's clock, each a length in the state's time and the events that take effect
+ * at its start, queued on the device and stepped by "slots" the caller enqueues (or captures into
+ * a CUDA graph once and replays every frame). A slot has three launches:
+ *   - begin: one thread. It settles the last slot (a landed tick's read-back record), and when no
+ *     tick is in flight and one is queued, begins it: the step's time left becomes its length.
+ *   - apply: one CTA. It writes the begun tick's events into the step's planes, in push order.
+ *   - the tick: one sub-step of min(stable step, time left), or nothing when no tick is in flight.
+ * Every sub-step's length is chosen on the device from the state alone, so the bytes are those of
+ * wl_advance(length) per tick with the events applied between, however many slots each call
+ * enqueues: a slot past the work changes nothing. A tick of length 0 carries its events alone.
+ * While a queue is attached, wl_run_steps, wl_enqueue_steps, wl_advance, wl_write_state(_device)
+ * and a coarser source clock are refused: the queue owns the step's clock (water_live.md:92). A
+ * queued tick's sub-steps read the bed, Manning's n and the source as they stand, so change them
+ * through events to keep a run's bytes independent of the slots. Destroy the queue before its
+ * step (wl_destroy of the step also detaches it). */
+typedef struct wl_queue wl_queue;
+
+enum {
+  WL_EVENT_BED = 0,    /* the bed's heights over the rectangle (metres, the step's f32 datum) */
+  WL_EVENT_SOURCE = 1, /* the source over the rectangle (m/s); the step must have a source on */
+  WL_EVENT_MANNING = 2 /* Manning's n over the rectangle; the step must have Manning on */
+};
+
+/* One event: a rectangle of one plane replaced by w * h values, row by row. */
+typedef struct wl_event {
+  uint32_t kind;
+  uint32_t x0, y0, w, h;
+} wl_event;
+
+/* What a landed tick leaves (water_live.md:94): its number, its sub-steps, its shortest and
+ * longest sub-step, and the ledger's time and step count when it landed. */
+typedef struct wl_landed {
+  uint32_t tick;
+  uint32_t substeps;
+  float shortest_s;
+  float longest_s;
+  float time_hi;
+  float time_lo;
+  uint32_t steps;
+  uint32_t events;
+} wl_landed;
+
+typedef struct wl_queue_status {
+  uint32_t pushed;  /* ticks pushed since the queue was made */
+  uint32_t begun;   /* ticks begun */
+  uint32_t landed;  /* ticks landed */
+  uint32_t active;  /* 1 while a begun tick has not landed */
+  uint32_t substeps; /* sub-steps of the tick in flight */
+  uint32_t pad[3];
+} wl_queue_status;
+
+/* A queue of `records` ticks (at most 64 in flight: water_live.md:84) over a step, with an event
+ * arena of `arena_values` floats and room for `max_events` events. */
+int wl_queue_create(wl_step* step, uint32_t records, uint32_t arena_values, uint32_t max_events,
+                    wl_queue** out, char* err, size_t err_len);
+void wl_queue_destroy(wl_queue* queue);
+/* Queues one tick: its number, its length (s, >= 0) and its events with their values, in order
+ * (sum of w * h values). Waits for the copy. WL_ERR_REFUSED when the ring, the event ring or the
+ * arena has no room yet: the caller keeps the tick and pushes it after slots have begun others. */
+int wl_queue_push(wl_queue* queue, uint32_t tick, float length_s, const wl_event* events,
+                  uint32_t n_events, const float* values, size_t n_values, char* err,
+                  size_t err_len);
+/* `slots` slots on `stream` (null: the step's own stream), no wait; graph-capturable. */
+int wl_queue_enqueue_slots(wl_queue* queue, wl_stream stream, uint32_t slots);
+/* The slots, then a wait. */
+int wl_queue_run_slots(wl_queue* queue, uint32_t slots, char* err, size_t err_len);
+int wl_queue_status_read(wl_queue* queue, wl_queue_status* out, char* err, size_t err_len);
+/* The read-back records of landed ticks first .. first + count - 1 (the 0-based landing order);
+ * the last `records` landings are kept. */
+int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_landed* out,
+                         char* err, size_t err_len);
+/* Launches a slot makes (3), and the queue's device bytes. */
+uint32_t wl_queue_launches_per_slot(void);
+uint64_t wl_queue_device_bytes(const wl_queue* queue);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -117,3 +117,20 @@ def test_the_numerics_policy_of_every_build():
     code = re.sub(r"//[^\n]*", "", update)
     assert not re.search(r"[\w)\]]\s*[-+*/]\s*[\w(]", re.sub(r"__f\w+_rn\(|\b\d+\.\d+f\b", "", code)
                          .replace("-added", "").replace("-target", "")), "a bare float operator"
+
+
+def test_a_queue_without_a_step_refuses_every_call(wl_lib):
+    # The tick queue's calls with no step or no queue: WL_ERR_INVALID (1), nothing touched.
+    err = C.create_string_buffer(128)
+    out = C.c_void_p()
+    assert wl_lib.wl_queue_create(None, 64, 1024, 16, C.byref(out), err, 128) == 1
+    assert not out.value
+    assert wl_lib.wl_queue_create(None, 64, 1024, 16, None, err, 128) == 8
+    assert wl_lib.wl_queue_push(None, 0, 0.01, None, 0, None, 0, err, 128) == 1
+    assert wl_lib.wl_queue_enqueue_slots(None, None, 4) == 1
+    assert wl_lib.wl_queue_run_slots(None, 4, err, 128) == 1
+    assert wl_lib.wl_queue_status_read(None, None, err, 128) == 1
+    assert wl_lib.wl_queue_read_landed(None, 0, 1, None, err, 128) == 1
+    assert wl_lib.wl_queue_launches_per_slot() == 3
+    assert wl_lib.wl_queue_device_bytes(None) == 0
+    wl_lib.wl_queue_destroy(None)

@@ -1,0 +1,217 @@
+"""The tick queue (the design of water_live.md:76-94, ADR-0081) against the oracle, bit for bit.
+
+A queued tick takes the sub-steps the oracle's advance takes for the same length, with its events
+written into the planes at its start, so after every tick has landed the state's four planes, the
+records and the ledger's sums equal the oracle's advance-per-tick run. The same bytes come out
+whatever number of slots each call runs ("the same bytes at any frame rate"), from a captured
+graph of slots, and through a ring that wraps; idle slots change nothing; each landed tick's
+read-back record carries the oracle's sub-step count.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cases
+from pairs import bits, make_pair
+from game_engine_gb300.tick_queue import (EVENT_BED, EVENT_MANNING, EVENT_SOURCE, ERR_REFUSED,
+                                          Event, TickQueue)
+
+pytestmark = pytest.mark.gpu
+TICK = float(np.float32(1.0 / 60.0))
+LEDGER_SUMS = ("source_m3", "open_edge_out_m3", "roundoff_m3", "time_s", "steps")
+
+
+def plan_for(c, n_ticks, seed):
+    """(tick, length, events) for n ticks of 1/60 s: bed, source and Manning patches, a tick of
+    no length that carries an event, and two overlapping patches in one tick."""
+    rng = np.random.default_rng(seed)
+    nx, ny = c["nx"], c["ny"]
+    plan = []
+    for t in range(n_ticks):
+        events = []
+        length = TICK
+        if t % 6 == 3:
+            w, h = int(rng.integers(1, min(nx, 9) + 1)), int(rng.integers(1, min(ny, 7) + 1))
+            x0, y0 = int(rng.integers(0, nx - w + 1)), int(rng.integers(0, ny - h + 1))
+            events.append(Event(EVENT_BED, x0, y0, rng.uniform(0.0, 0.4, (h, w))))
+        if t % 6 == 5 and c.get("source") is not None:
+            events.append(Event(EVENT_SOURCE, 2, 3, np.full((4, 5), 3e-3)))
+        if t % 9 == 7 and c.get("manning") is not None:
+            events.append(Event(EVENT_MANNING, 0, 0, np.full((ny, 3), 0.05)))
+        if t % 10 == 9:
+            length = 0.0
+            events.append(Event(EVENT_BED, 1, 1, np.full((2, 2), 0.7)))
+        if t % 10 == 4:
+            events.append(Event(EVENT_BED, 0, 0, np.full((3, 3), 0.2)))
+            events.append(Event(EVENT_BED, 1, 1, np.full((3, 3), 0.3)))  # the later one wins
+        plan.append((1000 + t, length, events))
+    return plan
+
+
+def oracle_run(ref, c, plan):
+    """The oracle: each tick's events into its planes, then advance(length). Returns the steps."""
+    planes = {EVENT_BED: np.asarray(c["bed"], np.float64).astype(np.float32)}
+    if c.get("source") is not None:
+        planes[EVENT_SOURCE] = np.asarray(c["source"], np.float64).astype(np.float32)
+    if c.get("manning") is not None:
+        planes[EVENT_MANNING] = np.asarray(c["manning"], np.float64).astype(np.float32)
+    nx, ny = c["nx"], c["ny"]
+    steps = []
+    for _, length, events in plan:
+        for e in events:
+            v = np.asarray(e.values, np.float32)
+            p = planes[e.kind].reshape(ny, nx)
+            p[e.y0:e.y0 + v.shape[0], e.x0:e.x0 + v.shape[1]] = v
+        for kind in {e.kind for e in events}:
+            wide = planes[kind].astype(np.float64)  # f32 values widen exactly; datum 0
+            {EVENT_BED: lambda: ref.set_bed(wide, 0.0), EVENT_SOURCE: lambda: ref.set_source(wide),
+             EVENT_MANNING: lambda: ref.set_manning(wide)}[kind]()
+        steps.append(ref.advance(length)[0] if length > 0 else 0)
+    return steps
+
+
+def device_run(q, n_ticks, partition, most_calls=20000):
+    """Slots in calls of the partition's sizes, in turn, until n ticks have landed."""
+    k = 0
+    for _ in range(most_calls):
+        st = q.status()
+        if st["landed"] >= n_ticks:
+            return
+        assert q.run_slots(partition[k % len(partition)]), q.error
+        k += 1
+    raise AssertionError("the queue did not land its ticks")
+
+
+def assert_same_after_ticks(dev, ref, what):
+    a, b = dev.read_state_bits(), ref.read_state_bits()
+    diff = np.nonzero(bits(a) != bits(b))[0]
+    assert diff.size == 0, f"{what}: {diff.size} state words differ, first at {diff[:5]}"
+    # The oracle's advance ends with a flush (the records' volumes folded into the ledger and
+    # cleared); read_ledger flushes the device's, so the records compare after it.
+    la, lb = dev.read_ledger(), ref.read_ledger()
+    for k in LEDGER_SUMS:
+        assert la[k] == lb[k], (what, k, la[k], lb[k])
+    assert np.array_equal(bits(dev.read_partials_bits()), bits(ref.read_partials_bits())), what
+
+
+@pytest.mark.parametrize("case", ["slope", "basin"])
+@pytest.mark.parametrize("partition", [[1], [3, 1, 7, 2], [200]])
+def test_queued_ticks_equal_advance_per_tick(gpu, case, partition):
+    c = cases.slope(False) if case == "slope" else cases.closed_basin()
+    dev, ref = make_pair(c)
+    n = 24
+    plan = plan_for(c, n, seed=11)
+    want_steps = oracle_run(ref, c, plan)
+    q = TickQueue(dev, records=32, arena_values=4096, max_events=64)
+    for tick, length, events in plan:
+        assert q.push(tick, length, events), q.error
+    device_run(q, n, partition)
+    assert_same_after_ticks(dev, ref, f"{case} {partition}")
+    landed = q.landed(0, n)
+    assert [r["tick"] for r in landed] == [t for t, _, _ in plan]
+    assert [r["substeps"] for r in landed] == want_steps
+    assert [r["events"] for r in landed] == [len(e) for _, _, e in plan]
+    for r in landed:
+        if r["substeps"]:
+            assert 0.0 < r["shortest_s"] <= r["longest_s"] <= TICK
+    st = q.status()
+    assert st == dict(pushed=n, begun=n, landed=n, active=0, substeps=st["substeps"])
+    # Idle slots change nothing.
+    h = dev.state_hash()
+    assert q.run_slots(9), q.error
+    assert dev.state_hash() == h and q.status()["landed"] == n
+    q.close()
+
+
+def test_the_queue_owns_the_clock(gpu):
+    dev, ref = make_pair(cases.closed_basin())
+    q = TickQueue(dev, records=8)
+    assert not dev.run_steps(1, 0.01) and dev.last_code == 5
+    assert dev.advance(0.1) == 0
+    assert not dev.set_source(np.zeros(dev.cell_count()), every=2)
+    q.close()
+    # Without the queue, the step's own calls again, and the clock free-running (no time left).
+    assert dev.run_steps(3, float("inf")), dev.error
+    ref.run_steps(3, float("inf"))
+    a, b = dev.read_state_bits(), ref.read_state_bits()
+    assert np.array_equal(bits(a), bits(b))
+    assert dev.read_ledger()["remaining_s"] == float("inf")
+
+
+def test_refusals_keep_the_queue_whole(gpu):
+    c = cases.slope(False)
+    dev, _ = make_pair(c)
+    q = TickQueue(dev, records=2, arena_values=64, max_events=4)
+    big = Event(EVENT_BED, 0, 0, np.zeros((9, 9)))  # 81 values: more than the arena
+    assert not q.push(1, TICK, [big]) and q.last_code == 2
+    off = Event(EVENT_BED, 45, 0, np.zeros((1, 4)))  # leaves the 48-wide grid
+    assert not q.push(1, TICK, [off]) and q.last_code == 2
+    assert q.push(1, TICK) and q.push(2, TICK)
+    assert not q.push(3, TICK) and q.last_code == ERR_REFUSED  # two records in flight
+    assert q.status()["pushed"] == 2
+    assert q.run_slots(1), q.error  # begins tick 1: its record's place is free
+    assert q.push(3, TICK), q.error
+    q.close()
+    d2, _ = make_pair(cases.closed_basin())  # no source, no Manning
+    q2 = TickQueue(d2, records=4)
+    assert not q2.push(1, TICK, [Event(EVENT_SOURCE, 0, 0, np.zeros((1, 1)))])
+    assert q2.last_code == 8
+    q2.close()
+
+
+def test_a_ring_that_wraps(gpu):
+    c = cases.slope(False)
+    dev, ref = make_pair(c)
+    n = 150
+    plan = plan_for(c, n, seed=5)
+    want = oracle_run(ref, c, plan)
+    q = TickQueue(dev, records=4, arena_values=256, max_events=8)
+    k = 0
+    for _ in range(100000):
+        while k < n and q.push(*plan[k]):
+            k += 1
+        if k < n:
+            assert q.last_code == ERR_REFUSED, q.error
+        if q.status()["landed"] == n:
+            break
+        assert q.run_slots(3), q.error
+    assert q.status()["landed"] == n
+    assert_same_after_ticks(dev, ref, "wrapped")
+    landed = q.landed(n - 4, 4)
+    assert [r["substeps"] for r in landed] == want[-4:]
+    assert q.landed(0, 1) is None  # landing 0 is no longer held
+    q.close()
+
+
+def test_slots_from_a_captured_graph(gpu):
+    import torch
+    c = cases.closed_basin()
+    dev, ref = make_pair(c)
+    n = 12
+    plan = plan_for(c, n, seed=3)
+    oracle_run(ref, c, plan)
+    q = TickQueue(dev, records=16)
+    for p in plan:
+        assert q.push(*p), q.error
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        assert q.enqueue_slots(torch.cuda.current_stream().cuda_stream, 4)
+    for _ in range(2000):
+        graph.replay()
+        torch.cuda.synchronize()
+        if q.status()["landed"] == n:
+            break
+    assert q.status()["landed"] == n
+    assert_same_after_ticks(dev, ref, "graph")
+    q.close()
+
+
+def test_a_new_state_is_refused_while_queued(gpu):
+    dev, _ = make_pair(cases.closed_basin())
+    q = TickQueue(dev, records=4)
+    n = dev.cell_count()
+    assert not dev.write_state(np.zeros(n), np.zeros(n), np.zeros(n)) and dev.last_code == 5
+    q.close()
+    assert dev.write_state(np.zeros(n), np.zeros(n), np.zeros(n)), dev.error
