@@ -2,7 +2,8 @@
 """Benchmark of the live-water tick on a GB300 (one JSON line on stdout).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload plain_2048|plain_256|tiles_4096|adjoint_512|tiles_256_adjoint]
+                    [--workload plain_2048|plain_256|tiles_4096|adjoint_512|tiles_256_adjoint|
+                               tick_queue]
 
 The metric is water cell-updates per second. A bench step is one pass of the workload over its
 configuration: for the default (plain_2048, the throughput configuration) 500 ticks of one
@@ -14,7 +15,7 @@ the ticks, and the read-back of the state, every step.
 Beside the headline (unless --no-extras): `batched`, the 4096-tile configuration in one persistent
 graph-captured launch a tick against the per-tile-launch form; `adjoint` and `batched_adjoint`, the
 checkpointed sweep's seconds per tick (forward and reverse) against the plain tick's on the same
-tiles.
+tiles; `tick_queue`, a captured frame of queue slots, busy and idle, against the plain tick.
 
 `--impl reference` times the reference's CPU tick (the FP64 solver, water_state::Solver::step,
 restated in oracle/ and checked byte for byte against the reference's own build) on this host's
@@ -452,6 +453,82 @@ def run_adjoint(steps: int, warmup: int, ticks: int = 0):
     }
 
 
+def run_tick_queue(steps: int, warmup: int, sides=(256, 2048), frame_slots: int = 16):
+    """The tick queue (water_live.md:76-94): ticks of 1/60 s queued on the device and stepped by
+    a captured graph of `frame_slots` slots (one frame's worth). Per tile side: microseconds a
+    busy slot (every slot steps), the plain tick's microseconds on the same tile and state, and
+    microseconds an idle slot (nothing queued)."""
+    import torch
+    from game_engine_gb300 import water_live as wl, workloads
+    from game_engine_gb300.tick_queue import TickQueue
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    tick = float(np.float32(1.0 / 60.0))
+    out = {"metric": "slot time", "unit": "us", "frame_slots": frame_slots,
+           "launches_per_slot": TickQueue.launches_per_slot(), "tiles": {}}
+    for side in sides:
+        t = workloads.plain_256() if side == 256 else workloads.plain_2048(side)
+
+        def make():
+            st = wl.DeviceStep()
+            assert st.create(wl.Config(t.nx, t.ny, t.cell_m, device=dev)), st.error
+            assert st.set_bed(t.bed) and st.write_state(t.h, t.hu, t.hv), st.error
+            if t.source is not None:
+                assert st.set_source(t.source), st.error
+            return st
+
+        # The plain tick on the same state: free-running sub-steps of the stable length.
+        plain = make()
+        s_ptr = plain.stream()
+        stream = torch.cuda.ExternalStream(s_ptr)
+        for _ in range(warmup):
+            assert plain.record(s_ptr, frame_slots, float("inf")), plain.error
+        plain_ms = _time_on(stream, lambda: plain.record(s_ptr, frame_slots, float("inf")), steps)
+        plain.destroy()
+
+        step = make()
+        q = TickQueue(step, records=64)
+        g_stream = torch.cuda.Stream(device=dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=g_stream):
+            assert q.enqueue_slots(torch.cuda.current_stream().cuda_stream, frame_slots)
+
+        def frame():  # a replay on the stream the events are recorded on
+            with torch.cuda.stream(g_stream):
+                graph.replay()
+
+        busy, n_tick = [], 0
+        for k in range(warmup + steps):
+            # 3 frames of ticks queued (a sub-step or more each), one frame's slots timed.
+            while q.status()["pushed"] - q.status()["landed"] < 3 * frame_slots:
+                assert q.push(n_tick, tick), q.error
+                n_tick += 1
+            before = int(step.read_ledger_bits()[10])  # the ledger's step count
+            ms = _time_on(g_stream, frame, 1)[0]
+            assert int(step.read_ledger_bits()[10]) - before == frame_slots  # every slot stepped
+            if k >= warmup:
+                busy.append(ms)
+        for _ in range(100000):  # drain
+            st = q.status()
+            if st["landed"] == st["pushed"]:
+                break
+            frame()
+            torch.cuda.synchronize()
+        idle = _time_on(g_stream, frame, steps)
+        landed = q.status()["landed"]
+        subs = [r["substeps"] for r in q.landed(max(0, landed - 16), min(16, landed))]
+        q.close()
+        step.destroy()
+        busy_us = statistics.median(busy) * 1e3 / frame_slots
+        plain_us = statistics.median(plain_ms) * 1e3 / frame_slots
+        out["tiles"][f"{t.nx}x{t.ny}"] = {
+            "busy_slot_us": busy_us, "plain_tick_us": plain_us,
+            "overhead_us": busy_us - plain_us, "idle_slot_us": statistics.median(idle) * 1e3 /
+            frame_slots, "cell_updates_per_s": t.cells / (busy_us * 1e-6),
+            "substeps_per_tick": subs, "ticks_landed": landed}
+    return out
+
+
 def run_tiles_adjoint(steps: int, warmup: int, ticks: int = 0, count: int = 256):
     """The batched adjoint configuration (256 tiles, 500 ticks, a checkpoint every 25, 64 probes
     a tile): the sweep over every tile in one launch a tick forward and reverse, from one captured
@@ -537,6 +614,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from game_engine_gb300 import workloads
 
+    if args.workload == "tick_queue":
+        if rank == 0:
+            print(json.dumps(run_tick_queue(args.steps, args.warmup)), flush=True)
+        return
     if args.workload in ("tiles_4096", "adjoint_512", "tiles_256_adjoint"):
         if rank == 0:
             fn = {"tiles_4096": run_tiles, "adjoint_512": run_adjoint,
@@ -570,6 +651,7 @@ def main():
         out["batched"] = run_tiles(max(1, min(args.steps, 3)), 1)
         out["adjoint"] = run_adjoint(max(1, min(args.steps, 3)), 1)
         out["batched_adjoint"] = run_tiles_adjoint(max(1, min(args.steps, 3)), 1)
+        out["tick_queue"] = run_tick_queue(max(3, min(args.steps, 10)), 3)
     if rank == 0:
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(tile, os.cpu_count() or 1)

@@ -512,7 +512,7 @@ int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_lan
   return WL_OK;
 }
 
-uint32_t wl_queue_launches_per_slot(void) { return 3u; }
+uint32_t wl_queue_launches_per_slot(void) { return 2u; }
 
 uint64_t wl_queue_device_bytes(const wl_queue* queue) {
   return queue != nullptr && queue->step != nullptr ? queue->q.device_bytes() : 0u;

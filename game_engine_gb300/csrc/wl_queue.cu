@@ -1,10 +1,11 @@
-// The tick queue's kernels and host side (wl_queue.h). A slot is three launches on one stream:
+// The tick queue's kernels and host side (wl_queue.h). A slot is two launches on one stream:
 //
-//   queue_begin_kernel  one thread: settles the last slot (counts its sub-step, lands a tick whose
-//                       time left reached zero, releases the events the last apply read), then,
-//                       when no tick is in flight and one is queued, begins it by setting the
-//                       step's time left to its length; writes the slot's `go` and `apply` words.
-//   queue_apply_kernel  one CTA: the begun tick's events into the step's planes, in push order.
+//   queue_slot_kernel   one CTA. Its thread 0 settles the last slot (counts its sub-step, lands a
+//                       tick whose time left reached zero, releases the events the last slot
+//                       applied), then, when no tick is in flight and one is queued, begins it by
+//                       setting the step's time left to its length, and writes the slot's `go`.
+//                       Then the CTA writes the begun tick's events into the step's planes, in
+//                       push order.
 //   the tick            the step's own persistent tick (wl_kernels.cu) with max_dt = +inf, so a
 //                       sub-step is min(stable step, time left); it returns at once when `go` is 0.
 //
@@ -62,9 +63,9 @@ __device__ void settle(QueueCtl* q, const TileCtl* ctl, wl_landed* landed, uint3
   if (q->active != 0u && !(l.remaining_s > 0.0f)) land(q, l, landed, records);
 }
 
-__global__ void queue_begin_kernel(QueueCtl* q, const QueueRecord* ring, TileCtl* ctl,
-                                   wl_landed* landed, uint32_t records, int may_begin) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Thread 0's part of a slot: the settle and the begin.
+__device__ void begin(QueueCtl* q, const QueueRecord* ring, TileCtl* ctl, wl_landed* landed,
+                      uint32_t records, int may_begin) {
   volatile QueueCtl* vq = q;
   settle(q, ctl, landed, records);
   const uint32_t head = vq->head;  // the host's word
@@ -88,15 +89,21 @@ __global__ void queue_begin_kernel(QueueCtl* q, const QueueRecord* ring, TileCtl
   q->go = q->active;
 }
 
-// The begun tick's events, one after another (a later event over the same cells wins). The host
-// checked every rectangle against the grid and every plane's presence when it pushed them.
-__global__ void __launch_bounds__(kApplyThreads) queue_apply_kernel(const QueueCtl* q,
-                                                                    const QueueEvent* events,
-                                                                    uint32_t max_events,
-                                                                    const float* arena,
-                                                                    uint32_t arena_values,
-                                                                    const TileDesc* T) {
-  if (q->apply == 0u) return;
+// A slot's first launch: thread 0's begin, then the begun tick's events by the whole CTA, one
+// after another (a later event over the same cells wins). The host checked every rectangle
+// against the grid and every plane's presence when it pushed them. With may_begin 0 it only
+// settles (the call's last launch, so a read-back after it sees the last slot's effects).
+__global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
+    QueueCtl* q, const QueueRecord* ring, TileCtl* ctl, wl_landed* landed, uint32_t records,
+    int may_begin, const QueueEvent* events, uint32_t max_events, const float* arena,
+    uint32_t arena_values, const TileDesc* T) {
+  __shared__ uint32_t s_apply;
+  if (threadIdx.x == 0) {
+    begin(q, ring, ctl, landed, records, may_begin);
+    s_apply = q->apply;
+  }
+  __syncthreads();
+  if (s_apply == 0u) return;
   const uint32_t n = q->events;
   const uint64_t first = q->first_event;
   for (uint32_t e = 0; e < n; ++e) {
@@ -300,18 +307,17 @@ cudaError_t TickQueue::enqueue(cudaStream_t s, uint32_t slots) {
   const TileDesc& d = set_->desc(0);
   const float inf = std::numeric_limits<float>::infinity();
   for (uint32_t k = 0; k < slots; ++k) {
-    queue_begin_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 1);
+    queue_slot_kernel<<<1, kApplyThreads, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 1,
+                                                   d_events_, max_events_, d_arena_, arena_,
+                                                   set_->device_descs());
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    queue_apply_kernel<<<1, kApplyThreads, 0, s>>>(d_ctl_, d_events_, max_events_, d_arena_,
-                                                    arena_, set_->device_descs());
-    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = set_->enqueue_ticks(s, 1, inf, &d_ctl_->go);
     if (e != cudaSuccess) return e;
   }
   // The last slot's effects, so a read-back after the call sees them.
-  queue_begin_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 0);
+  queue_slot_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 0, d_events_,
+                                     max_events_, d_arena_, arena_, set_->device_descs());
   return cudaGetLastError();
 }
 

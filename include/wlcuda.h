@@ -314,11 +314,12 @@ int wl_tick_noalloc(const wl_config* config, int fixed_ops, const float* planes_
  *
  * Ticks of the world's clock, each a length in the state's time and the events that take effect
  * at its start, queued on the device and stepped by "slots" the caller enqueues (or captures into
- * a CUDA graph once and replays every frame). A slot has three launches:
- *   - begin: one thread. It settles the last slot (a landed tick's read-back record), and when no
- *     tick is in flight and one is queued, begins it: the step's time left becomes its length.
- *   - apply: one CTA. It writes the begun tick's events into the step's planes, in push order.
+ * a CUDA graph once and replays every frame). A slot has two launches:
+ *   - begin and apply, one CTA: it settles the last slot (a landed tick's read-back record), and
+ *     when no tick is in flight and one is queued, begins it (the step's time left becomes its
+ *     length) and writes its events into the step's planes, in push order.
  *   - the tick: one sub-step of min(stable step, time left), or nothing when no tick is in flight.
+ * A call adds one more launch after its slots, which settles the last of them.
  * Every sub-step's length is chosen on the device from the state alone, so the bytes are those of
  * wl_advance(length) per tick with the events applied between, however many slots each call
  * enqueues: a slot past the work changes nothing. A tick of length 0 carries its events alone.
@@ -383,7 +384,7 @@ int wl_queue_status_read(wl_queue* queue, wl_queue_status* out, char* err, size_
  * the last `records` landings are kept. */
 int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_landed* out,
                          char* err, size_t err_len);
-/* Launches a slot makes (3), and the queue's device bytes. */
+/* Launches a slot makes (2), and the queue's device bytes. */
 uint32_t wl_queue_launches_per_slot(void);
 uint64_t wl_queue_device_bytes(const wl_queue* queue);
 

@@ -131,6 +131,6 @@ def test_a_queue_without_a_step_refuses_every_call(wl_lib):
     assert wl_lib.wl_queue_run_slots(None, 4, err, 128) == 1
     assert wl_lib.wl_queue_status_read(None, None, err, 128) == 1
     assert wl_lib.wl_queue_read_landed(None, 0, 1, None, err, 128) == 1
-    assert wl_lib.wl_queue_launches_per_slot() == 3
+    assert wl_lib.wl_queue_launches_per_slot() == 2
     assert wl_lib.wl_queue_device_bytes(None) == 0
     wl_lib.wl_queue_destroy(None)
