@@ -441,3 +441,145 @@ def adj_loss64(grid: Grid, dt, ticks, bed, source, state0, probes, targets):
 def hash_floats(values) -> int:
     v = np.ascontiguousarray(values, dtype=np.float32)
     return int(lib().oracle_hash_floats(v.ctypes.data_as(_fp), v.size))
+
+
+# ---- the complete FP64 step (ws_oracle.hpp), and the reference's own build of it ------------
+
+_FULL_FIELDS = dict(depth=0, momentum_x=1, momentum_y=2, ground=3, carried=4, speed=5,
+                    bed_stress_x=6, bed_stress_y=7, dissipation=8)
+_INPUT_KEYS = ("bed", "manning", "source", "ground_k", "ground_s", "ground_cap")
+LEDGER_KEYS = ("source_m3", "open_edge_out_m3", "ground_m3", "roundoff_m3", "scheme_loss_j",
+               "friction_work_j", "time_s", "steps")
+CARRIED_LEDGER_KEYS = ("source", "from_dissipation", "exchange", "decayed", "open_edge_out")
+
+
+def _bind_full(L, prefix):
+    f = getattr(L, prefix + "create")
+    f.restype = C.c_void_p
+    f.argtypes = [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_double,
+                  C.c_double, C.c_uint32, C.c_uint32, _dp]
+    for name, res, args in [("destroy", None, [C.c_void_p]),
+                            ("set", None, [C.c_void_p, C.c_int, _dp]),
+                            ("get", None, [C.c_void_p, C.c_int, _dp]),
+                            ("step", C.c_double, [C.c_void_p, C.c_void_p, C.c_double]),
+                            ("advance", C.c_uint64, [C.c_void_p, C.c_void_p, C.c_double]),
+                            ("ledger", None, [C.c_void_p, _dp]),
+                            ("hash", C.c_uint64, [C.c_void_p])]:
+        g = getattr(L, prefix + name)
+        g.restype = res
+        g.argtypes = args
+
+
+class FullSolver:
+    """water_state::Solver complete (water_state.h:161-266): the oracle's restatement, or with
+    reference=True the reference's own build (oracle/_ref, where its sources were present).
+
+    `carried` lists each quantity's (decay_s, per_joule, min_speed_m_per_s). Inputs are a dict:
+    bed, manning, source, ground_k, ground_s, ground_cap (arrays or None), carried_source and
+    carried_exchange (lists of arrays or None, one a quantity)."""
+
+    def __init__(self, nx, ny, cell_m=1.0, gravity=9.81, cfl=0.45, dry=1e-9, rho=1000.0,
+                 open_edges=0, carried=(), reference=False):
+        self._L = ref() if reference else lib()
+        self._p = "wsref_full_" if reference else "oracle_ws_"
+        if not hasattr(self._L, "_full_bound"):
+            _bind_full(self._L, self._p)
+            self._L._full_bound = True
+        self.nx, self.ny, self.k = int(nx), int(ny), len(carried)
+        cc = np.zeros(12)
+        for i, c in enumerate(carried):
+            cc[3 * i:3 * i + 3] = c
+        self._cc = cc
+        self.h = getattr(self._L, self._p + "create")(self.nx, self.ny, cell_m, gravity, cfl, dry,
+                                                      rho, int(open_edges), self.k,
+                                                      cc.ctypes.data_as(_dp))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            getattr(self._L, self._p + "destroy")(self.h)
+            self.h = None
+
+    @property
+    def cells(self):
+        return self.nx * self.ny
+
+    def _size(self, field):
+        return self.cells * (self.k if field == "carried" else 1)
+
+    def set(self, field, values):
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        assert v.size == self._size(field), field
+        getattr(self._L, self._p + "set")(self.h, _FULL_FIELDS[field], v.ctypes.data_as(_dp))
+
+    def get(self, field):
+        out = np.zeros(self._size(field))
+        if out.size:
+            getattr(self._L, self._p + "get")(self.h, _FULL_FIELDS[field], out.ctypes.data_as(_dp))
+        return out
+
+    def _inputs(self, inputs):
+        keep = []
+        ptrs = (C.c_void_p * 14)()
+        for j, key in enumerate(_INPUT_KEYS):
+            a = inputs.get(key)
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                keep.append(a)
+                ptrs[j] = a.ctypes.data
+        for off, key in ((6, "carried_source"), (10, "carried_exchange")):
+            for k, a in enumerate(inputs.get(key) or ()):
+                if a is not None:
+                    a = np.ascontiguousarray(a, dtype=np.float64)
+                    keep.append(a)
+                    ptrs[off + k] = a.ctypes.data
+        return ptrs, keep
+
+    def step(self, inputs, max_dt):
+        ptrs, keep = self._inputs(inputs)
+        return getattr(self._L, self._p + "step")(self.h, ptrs, float(max_dt))
+
+    def advance(self, inputs, duration):
+        ptrs, keep = self._inputs(inputs)
+        return int(getattr(self._L, self._p + "advance")(self.h, ptrs, float(duration)))
+
+    def ledger(self):
+        out = np.zeros(28)
+        getattr(self._L, self._p + "ledger")(self.h, out.ctypes.data_as(_dp))
+        d = dict(zip(LEDGER_KEYS, out[:8]))
+        d["steps"] = int(d["steps"])
+        d["carried"] = [dict(zip(CARRIED_LEDGER_KEYS, out[8 + 5 * k:13 + 5 * k]))
+                        for k in range(self.k)]
+        return d
+
+    def state_hash(self):
+        return int(getattr(self._L, self._p + "hash")(self.h))
+
+
+def fd_exp(x):
+    """fdlibm's e^x as the oracle restates it (ws_oracle.hpp)."""
+    L = lib()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    L.oracle_fd_exp_n.argtypes = [_dp, _dp, C.c_size_t]
+    L.oracle_fd_exp_n(x.ctypes.data_as(_dp), out.ctypes.data_as(_dp), x.size)
+    return out
+
+
+def fd_log(x):
+    L = lib()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    L.oracle_fd_log_n.argtypes = [_dp, _dp, C.c_size_t]
+    L.oracle_fd_log_n(x.ctypes.data_as(_dp), out.ctypes.data_as(_dp), x.size)
+    return out
+
+
+def ref_det(name, x):
+    """The reference's own det::exp or det::log (core/math/include/core/math/deterministic.h)."""
+    R = ref()
+    f = getattr(R, f"wsref_det_{name}_n")
+    f.argtypes = [_dp, _dp, C.c_size_t]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    f(x.ctypes.data_as(_dp), out.ctypes.data_as(_dp), x.size)
+    return out

@@ -330,3 +330,117 @@ double oracle_adj_loss64(uint32_t nx, uint32_t ny, double cell_m, double gravity
 }
 
 }  // extern "C"
+
+// ---- the complete FP64 step (ws_oracle.hpp) ----------------------------------------------------
+//
+// Inputs come as 14 pointers, null for an empty span: bed, manning, source, ground conductivity,
+// ground suction, ground capacity, carried source 0-3, carried exchange 0-3.
+
+#include "ws_oracle.hpp"
+
+namespace {
+
+ws_oracle::Inputs ws_inputs(const double* const* p) {
+  ws_oracle::Inputs in;
+  in.bed = p[0];
+  in.manning = p[1];
+  in.source = p[2];
+  in.ground_k = p[3];
+  in.ground_s = p[4];
+  in.ground_cap = p[5];
+  for (int k = 0; k < 4; ++k) {
+    in.carried_source[k] = p[6 + k];
+    in.carried_exchange[k] = p[10 + k];
+  }
+  return in;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* oracle_ws_create(uint32_t nx, uint32_t ny, double cell_m, double gravity, double cfl,
+                       double dry, double rho, uint32_t open_edges, uint32_t carried,
+                       const double* cc) {
+  ws_oracle::Config c;
+  c.nx = nx;
+  c.ny = ny;
+  c.cell_m = cell_m;
+  c.gravity = gravity;
+  c.cfl = cfl;
+  c.dry = dry;
+  c.rho = rho;
+  c.carried = carried;
+  for (uint32_t k = 0; k < carried && k < 4; ++k) c.cc[k] = {cc[3 * k], cc[3 * k + 1], cc[3 * k + 2]};
+  c.west_open = open_edges & 1u;
+  c.east_open = open_edges & 2u;
+  c.south_open = open_edges & 4u;
+  c.north_open = open_edges & 8u;
+  return new (std::nothrow) ws_oracle::SolverFull(c);
+}
+
+void oracle_ws_destroy(void* p) { delete static_cast<ws_oracle::SolverFull*>(p); }
+
+// which: 0 depth, 1 momentum x, 2 momentum y, 3 ground, 4 carried (k * n), 5 speed, 6 bed
+// stress x, 7 bed stress y, 8 dissipation.
+static std::vector<double>& ws_field(ws_oracle::SolverFull* s, int which) {
+  switch (which) {
+    case 0: return s->h;
+    case 1: return s->hu;
+    case 2: return s->hv;
+    case 3: return s->ground;
+    case 4: return s->carried;
+    case 5: return s->speed;
+    case 6: return s->tau_x;
+    case 7: return s->tau_y;
+    default: return s->dissipation;
+  }
+}
+
+void oracle_ws_set(void* p, int which, const double* v) {
+  auto* s = static_cast<ws_oracle::SolverFull*>(p);
+  std::vector<double>& f = ws_field(s, which);
+  std::memcpy(f.data(), v, f.size() * sizeof(double));
+}
+
+void oracle_ws_get(void* p, int which, double* out) {
+  auto* s = static_cast<ws_oracle::SolverFull*>(p);
+  const std::vector<double>& f = ws_field(s, which);
+  std::memcpy(out, f.data(), f.size() * sizeof(double));
+}
+
+double oracle_ws_step(void* p, const double* const* inputs, double max_dt) {
+  return static_cast<ws_oracle::SolverFull*>(p)->step(ws_inputs(inputs), max_dt);
+}
+
+uint64_t oracle_ws_advance(void* p, const double* const* inputs, double duration) {
+  return static_cast<ws_oracle::SolverFull*>(p)->advance(ws_inputs(inputs), duration);
+}
+
+double oracle_ws_stable_step(void* p) { return static_cast<ws_oracle::SolverFull*>(p)->stable_step(); }
+
+// source, open, ground, roundoff, scheme_loss, friction, time, steps, then per carried quantity
+// source, from_dissipation, exchange, decayed, open (28 doubles).
+void oracle_ws_ledger(void* p, double* out) {
+  const ws_oracle::Ledger& l = static_cast<ws_oracle::SolverFull*>(p)->ledger;
+  const double head[8] = {l.source, l.open, l.ground, l.roundoff, l.scheme_loss, l.friction,
+                          l.time, double(l.steps)};
+  std::memcpy(out, head, sizeof head);
+  for (int k = 0; k < 4; ++k) {
+    const ws_oracle::CarriedLedger& c = l.carried[k];
+    const double v[5] = {c.source, c.from_dissipation, c.exchange, c.decayed, c.open};
+    std::memcpy(out + 8 + 5 * k, v, sizeof v);
+  }
+}
+
+uint64_t oracle_ws_hash(void* p) { return static_cast<ws_oracle::SolverFull*>(p)->state_hash(); }
+
+void oracle_fd_exp_n(const double* x, double* out, size_t n) {
+  for (size_t i = 0; i < n; ++i) out[i] = ws_oracle::fd_exp(x[i]);
+}
+
+void oracle_fd_log_n(const double* x, double* out, size_t n) {
+  for (size_t i = 0; i < n; ++i) out[i] = ws_oracle::fd_log(x[i]);
+}
+
+}  // extern "C"
