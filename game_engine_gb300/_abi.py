@@ -85,6 +85,35 @@ class QueueStatus(C.Structure):
                 ("active", C.c_uint32), ("substeps", C.c_uint32), ("pad", C.c_uint32 * 3)]
 
 
+class WsCarriedConfig(C.Structure):
+    """ws_carried_config: water_state::CarriedConfig (water_state.h:66-78)."""
+    _fields_ = [("decay_s", C.c_double), ("per_joule", C.c_double),
+                ("min_speed_m_per_s", C.c_double)]
+
+
+class WsConfig(C.Structure):
+    """ws_config: water_state::Config (water_state.h:83-99)."""
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("cell_m", C.c_double),
+                ("gravity", C.c_double), ("cfl", C.c_double), ("dry_depth_m", C.c_double),
+                ("water_density", C.c_double), ("carried", C.c_uint32), ("pad", C.c_uint32),
+                ("carried_config", WsCarriedConfig * 4), ("west_open", C.c_uint8),
+                ("east_open", C.c_uint8), ("south_open", C.c_uint8), ("north_open", C.c_uint8),
+                ("device", C.c_int32)]
+
+
+class WsCarriedLedger(C.Structure):
+    _fields_ = [("source", C.c_double), ("from_dissipation", C.c_double),
+                ("exchange", C.c_double), ("decayed", C.c_double), ("open_edge_out", C.c_double)]
+
+
+class WsLedger(C.Structure):
+    """ws_ledger: water_state::Ledger (water_state.h:135-145)."""
+    _fields_ = [("source_m3", C.c_double), ("open_edge_out_m3", C.c_double),
+                ("ground_m3", C.c_double), ("roundoff_m3", C.c_double),
+                ("scheme_loss_j", C.c_double), ("friction_work_j", C.c_double),
+                ("time_s", C.c_double), ("steps", C.c_uint64), ("carried", WsCarriedLedger * 4)]
+
+
 _u64p = C.POINTER(C.c_uint64)
 _u32p = C.POINTER(C.c_uint32)
 
@@ -166,6 +195,27 @@ SIGNATURES = {
                                        *_err]),
     "wl_queue_launches_per_slot": (C.c_uint32, []),
     "wl_queue_device_bytes": (C.c_uint64, [C.c_void_p]),
+    # the complete FP64 step
+    "ws_create": (C.c_int, [C.POINTER(WsConfig), C.POINTER(C.c_void_p), *_err]),
+    "ws_destroy": (None, [C.c_void_p]),
+    "ws_valid": (C.c_int, [C.c_void_p]),
+    "ws_cell_count": (C.c_uint32, [C.c_void_p]),
+    "ws_write_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t, *_err]),
+    "ws_read_field": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t, *_err]),
+    "ws_set_input": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_size_t, *_err]),
+    "ws_stable_step": (C.c_double, [C.c_void_p, *_err]),
+    "ws_step": (C.c_double, [C.c_void_p, C.c_double, *_err]),
+    "ws_enqueue_steps": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32, C.c_double]),
+    "ws_run_steps": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, *_err]),
+    "ws_advance": (C.c_uint64, [C.c_void_p, C.c_double, *_err]),
+    "ws_read_ledger": (C.c_int, [C.c_void_p, C.POINTER(WsLedger), *_err]),
+    "ws_reset_ledger": (C.c_int, [C.c_void_p, *_err]),
+    "ws_surface_volume_m3": (C.c_double, [C.c_void_p, *_err]),
+    "ws_ground_volume_m3": (C.c_double, [C.c_void_p, *_err]),
+    "ws_carried_total": (C.c_double, [C.c_void_p, C.c_uint32, *_err]),
+    "ws_state_hash": (C.c_uint64, [C.c_void_p, *_err]),
+    "ws_stream": (wl_stream, [C.c_void_p]),
+    "ws_device_bytes": (C.c_uint64, [C.c_void_p]),
 }
 
 

@@ -20,9 +20,10 @@ OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libwlcuda.so")
 
-SOURCES = ["wl_kernels.cu", "wl_adjoint.cu", "wl_static.cu", "wl_queue.cu", "wl_tiles.cpp",
-           "wl_api.cpp", "wl_batch.cpp", "wl_util.cpp"]
-HEADERS = ["wl_device.cuh", "wl_kernels.h", "wl_tiles.h", "wl_adjoint.h", "wl_queue.h"]
+SOURCES = ["wl_kernels.cu", "wl_adjoint.cu", "wl_static.cu", "wl_queue.cu", "ws_solver.cu",
+           "wl_tiles.cpp", "wl_api.cpp", "wl_batch.cpp", "wl_util.cpp"]
+HEADERS = ["wl_device.cuh", "wl_kernels.h", "wl_tiles.h", "wl_adjoint.h", "wl_queue.h",
+           "ws_solver.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NUMERICS = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]

@@ -388,6 +388,102 @@ int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_lan
 uint32_t wl_queue_launches_per_slot(void);
 uint64_t wl_queue_device_bytes(const wl_queue* queue);
 
+/* ---- the complete FP64 step: engine::water_state::Solver on the device -------------------------
+ *
+ * domain/water_state/include/domain/water_state/water_state.h:161-266 and
+ * domain/water_state/src/water_state.cpp, with every input and output the reference's CPU step
+ * has and the live tick lacks: the ground's store by Green and Ampt, up to four carried
+ * quantities (decay, a source from the dissipation, an outside source, an exchange with the bed),
+ * the per-cell speed, bed stress and dissipation, and the whole ledger. The arithmetic is IEEE
+ * double in the reference's operand order with no contraction, and its cube root and decay take
+ * fdlibm's e^x and ln x as the reference's deterministic transcendentals do, so a step's bytes
+ * (state, outputs, ledger) equal the reference's CPU Solver's. Inputs are held on the device
+ * between steps (set once, changed with ws_set_input); the reference takes them with each step. */
+typedef struct ws_solver ws_solver;
+
+typedef struct ws_carried_config { /* water_state.h:66-78 */
+  double decay_s;
+  double per_joule;
+  double min_speed_m_per_s;
+} ws_carried_config;
+
+typedef struct ws_config { /* water_state.h:83-99; rows_per_job is not read */
+  uint32_t nx;
+  uint32_t ny;
+  double cell_m;
+  double gravity;
+  double cfl;
+  double dry_depth_m;
+  double water_density;
+  uint32_t carried; /* carried quantities in use, at most 4 */
+  uint32_t pad;
+  ws_carried_config carried_config[4];
+  uint8_t west_open; /* water_state::Edge: 0 closed, 1 open */
+  uint8_t east_open;
+  uint8_t south_open;
+  uint8_t north_open;
+  int32_t device;
+} ws_config;
+
+typedef struct ws_carried_ledger { /* water_state.h:124-130 */
+  double source, from_dissipation, exchange, decayed, open_edge_out;
+} ws_carried_ledger;
+
+typedef struct ws_ledger { /* water_state.h:135-145 */
+  double source_m3, open_edge_out_m3, ground_m3, roundoff_m3, scheme_loss_j, friction_work_j;
+  double time_s;
+  uint64_t steps;
+  ws_carried_ledger carried[4];
+} ws_ledger;
+
+/* The fields (water_state.h:147-160): the state, then the last step's outputs (read only). */
+enum {
+  WS_DEPTH = 0, WS_MOMENTUM_X = 1, WS_MOMENTUM_Y = 2, WS_GROUND = 3,
+  WS_CARRIED = 4, /* carried * nx * ny values, quantity after quantity */
+  WS_SPEED = 5, WS_BED_STRESS_X = 6, WS_BED_STRESS_Y = 7, WS_DISSIPATION = 8
+};
+/* The inputs (water_state.h:103-120). */
+enum {
+  WS_BED = 0, WS_MANNING = 1, WS_SOURCE = 2, WS_GROUND_CONDUCTIVITY = 3, WS_GROUND_SUCTION = 4,
+  WS_GROUND_CAPACITY = 5,
+  WS_CARRIED_SOURCE = 6,  /* + k for quantity k */
+  WS_CARRIED_EXCHANGE = 10 /* + k */
+};
+
+/* Solver::Solver (cpp:110-148): every array allocated once, the state zero, the ledger empty. */
+int ws_create(const ws_config* config, ws_solver** out, char* err, size_t err_len);
+void ws_destroy(ws_solver* solver);
+int ws_valid(const ws_solver* solver);
+uint32_t ws_cell_count(const ws_solver* solver);
+/* depth() ... carried(k) (water_state.h:167-180): n = the field's size. */
+int ws_write_field(ws_solver* solver, int field, const double* values, size_t n, char* err,
+                   size_t err_len);
+int ws_read_field(ws_solver* solver, int field, double* out, size_t n, char* err, size_t err_len);
+/* One of Inputs' spans, kept on the device: n = nx * ny, or 0 for an empty span. */
+int ws_set_input(ws_solver* solver, int input, const double* values, size_t n, char* err,
+                 size_t err_len);
+/* Solver::stable_step (cpp:211-224); 0 on an error. */
+double ws_stable_step(ws_solver* solver, char* err, size_t err_len);
+/* Solver::step (cpp:503-533): the length taken; 0 when the inputs do not fit (no bed, or the
+ * ground's three spans not all set or all empty) or max_dt <= 0, nothing changed then. */
+double ws_step(ws_solver* solver, double max_dt, char* err, size_t err_len);
+/* `count` steps on `stream` (null: the solver's own), no wait; graph-capturable. WL_ERR_SIZE when
+ * the inputs do not fit, WL_ERR_ARGUMENT for max_dt <= 0. */
+int ws_enqueue_steps(ws_solver* solver, wl_stream stream, uint32_t count, double max_dt);
+int ws_run_steps(ws_solver* solver, uint32_t count, double max_dt, char* err, size_t err_len);
+/* Solver::advance (cpp:535-547): the steps taken; 0 when the inputs do not fit. */
+uint64_t ws_advance(ws_solver* solver, double duration_s, char* err, size_t err_len);
+int ws_read_ledger(ws_solver* solver, ws_ledger* out, char* err, size_t err_len);
+int ws_reset_ledger(ws_solver* solver, char* err, size_t err_len);
+/* The volumes (cpp:549-568): sums in index order times a cell's area. */
+double ws_surface_volume_m3(ws_solver* solver, char* err, size_t err_len);
+double ws_ground_volume_m3(ws_solver* solver, char* err, size_t err_len);
+double ws_carried_total(ws_solver* solver, uint32_t k, char* err, size_t err_len);
+/* Solver::state_hash (cpp:570-578). 0 on an error. */
+uint64_t ws_state_hash(ws_solver* solver, char* err, size_t err_len);
+wl_stream ws_stream(ws_solver* solver);
+uint64_t ws_device_bytes(const ws_solver* solver);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -24,7 +24,7 @@ def declared_symbols():
             continue
         text = open(os.path.join(ROOT, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        names |= set(re.findall(r"\b(wl\w*)\s*\(", text))
+        names |= set(re.findall(r"\b((?:wl|ws)_\w*)\s*\(", text))
     return names
 
 
@@ -134,3 +134,25 @@ def test_a_queue_without_a_step_refuses_every_call(wl_lib):
     assert wl_lib.wl_queue_launches_per_slot() == 2
     assert wl_lib.wl_queue_device_bytes(None) == 0
     wl_lib.wl_queue_destroy(None)
+
+
+def test_a_full_solver_never_created_refuses_every_call(wl_lib):
+    # The complete FP64 step's calls with no solver: WL_ERR_INVALID (1), 0 for the value calls.
+    err = C.create_string_buffer(128)
+    assert wl_lib.ws_valid(None) == 0
+    assert wl_lib.ws_cell_count(None) == 0
+    assert wl_lib.ws_write_field(None, 0, None, 0, err, 128) == 1
+    assert wl_lib.ws_set_input(None, 0, None, 0, err, 128) == 1
+    assert wl_lib.ws_step(None, 0.1, err, 128) == 0.0
+    assert wl_lib.ws_advance(None, 1.0, err, 128) == 0
+    assert wl_lib.ws_enqueue_steps(None, None, 1, 0.1) == 1
+    assert wl_lib.ws_state_hash(None, err, 128) == 0
+    assert wl_lib.ws_read_ledger(None, None, err, 128) == 1
+    wl_lib.ws_destroy(None)
+    cfg = _abi.WsConfig()
+    cfg.nx, cfg.ny = 0, 4
+    out = C.c_void_p()
+    assert wl_lib.ws_create(C.byref(cfg), C.byref(out), err, 128) == 2 and not out.value
+    cfg.nx, cfg.carried = 4, 5
+    assert wl_lib.ws_create(C.byref(cfg), C.byref(out), err, 128) == 8 and not out.value
+    assert C.sizeof(_abi.WsConfig) == 160 and C.sizeof(_abi.WsLedger) == 224
