@@ -3,7 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload plain_2048|plain_256|tiles_4096|adjoint_512|tiles_256_adjoint|
-                               tick_queue]
+                               tick_queue|full_step]
 
 The metric is water cell-updates per second. A bench step is one pass of the workload over its
 configuration: for the default (plain_2048, the throughput configuration) 500 ticks of one
@@ -15,7 +15,9 @@ the ticks, and the read-back of the state, every step.
 Beside the headline (unless --no-extras): `batched`, the 4096-tile configuration in one persistent
 graph-captured launch a tick against the per-tile-launch form; `adjoint` and `batched_adjoint`, the
 checkpointed sweep's seconds per tick (forward and reverse) against the plain tick's on the same
-tiles; `tick_queue`, a captured frame of queue slots, busy and idle, against the plain tick.
+tiles; `tick_queue`, a captured frame of queue slots, busy and idle, against the plain tick;
+`full_step`, the complete FP64 step (ground store, carried quantities, outputs) on the device
+against the reference's CPU step restated in oracle/.
 
 `--impl reference` times the reference's CPU tick (the FP64 solver, water_state::Solver::step,
 restated in oracle/ and checked byte for byte against the reference's own build) on this host's
@@ -529,6 +531,76 @@ def run_tick_queue(steps: int, warmup: int, sides=(256, 2048), frame_slots: int 
     return out
 
 
+def full_step_workload(side: int = 2048):
+    """The complete FP64 step's workload: the throughput tile's terrain and depth with every input
+    on: Manning's n 0.03, the rain, a ground store (Green-Ampt K 5e-6 m/s, suction 0.08 m,
+    capacity 0.1 m), a foam made by the dissipation (decay 30 s) and a settling sediment."""
+    from game_engine_gb300 import workloads
+    t = workloads.plain_2048(side)
+    n = t.cells
+    config = dict(nx=t.nx, ny=t.ny, cell_m=t.cell_m, carried=[(30.0, 1e-4, 0.05), (0.0, 0.0, 0.0)])
+    fields = dict(depth=t.h, momentum_x=t.hu, momentum_y=t.hv, ground=np.zeros(n),
+                  carried=np.concatenate([np.zeros(n), 0.01 * t.h]))
+    inputs = dict(bed=t.bed, manning=np.full(n, 0.03), source=t.source,
+                  ground_k=np.full(n, 5e-6), ground_s=np.full(n, 0.08), ground_cap=np.full(n, 0.1),
+                  carried_source=[None, None], carried_exchange=[None, np.full(n, -1e-6)])
+    return t, config, fields, inputs
+
+
+def run_full_step(steps: int, warmup: int, side: int = 2048, ticks: int = 20, cpu_budget_s=10.0):
+    """The complete FP64 step (water_state::Solver with every input) on the device: seconds a step
+    and cell-updates/s over `ticks` steps of max_dt 0.01 from the same state, against the oracle's
+    restatement of the reference's CPU step on one host core, a bounded sample of steps."""
+    import torch
+    from game_engine_gb300 import water_state as ws
+    dev_index = int(os.environ.get("LOCAL_RANK", "0"))
+    t, config, fields, inputs = full_step_workload(side)
+    s = ws.Solver(ws.Config(config["nx"], config["ny"], config["cell_m"], carried=config["carried"],
+                            device=dev_index))
+    for name, v in fields.items():
+        s.set(name, v)
+    s.set_inputs(inputs)
+    stream = torch.cuda.ExternalStream(s.stream())
+    snapshot = {name: s.get(name) for name in fields}
+
+    def run():
+        assert s.enqueue_steps(s.stream(), ticks, 0.01)
+
+    for _ in range(warmup):
+        run()
+    torch.cuda.synchronize()
+    ms = _time_on(stream, run, steps)
+    launches = ticks * 6 + 1
+    device_bytes = s.device_bytes()
+    s.close()
+    step_s = statistics.median(ms) * 1e-3 / ticks
+    out = {"workload": f"the complete FP64 step, {t.nx}x{t.ny}: {t.meta['data']}; Manning 0.03, "
+                       "a ground store, a foam and a sediment; max_dt 0.01 s",
+           "metric": "cell-updates/s", "value": t.cells / step_s, "unit": "cell-updates/s",
+           "s_per_step": step_s, "steps_per_run": ticks, "gpu_launches_per_run": launches,
+           "device_bytes": device_bytes, "dtype": "f64"}
+    try:
+        import oracle
+        o = oracle.FullSolver(config["nx"], config["ny"], config["cell_m"],
+                              carried=config["carried"])
+        for name, v in snapshot.items():
+            o.set(name, v)
+        o.step(inputs, 0.01)  # untimed
+        n_cpu, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < cpu_budget_s and n_cpu < ticks:
+            o.step(inputs, 0.01)
+            n_cpu += 1
+        cpu_s = (time.perf_counter() - t0) / max(n_cpu, 1)
+        out["cpu_baseline"] = {"value": t.cells / cpu_s, "unit": "cell-updates/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"{n_cpu} steps of the same tile (after 1 untimed), the "
+                                         "reference's complete FP64 step restated in oracle/, one "
+                                         "thread"}
+    except Exception as e:  # the oracle is test infrastructure; the number is reported if it runs
+        out["cpu_baseline"] = {"unavailable": str(e)[:200]}
+    return out
+
+
 def run_tiles_adjoint(steps: int, warmup: int, ticks: int = 0, count: int = 256):
     """The batched adjoint configuration (256 tiles, 500 ticks, a checkpoint every 25, 64 probes
     a tile): the sweep over every tile in one launch a tick forward and reverse, from one captured
@@ -618,6 +690,10 @@ def main():
         if rank == 0:
             print(json.dumps(run_tick_queue(args.steps, args.warmup)), flush=True)
         return
+    if args.workload == "full_step":
+        if rank == 0:
+            print(json.dumps(run_full_step(args.steps, args.warmup)), flush=True)
+        return
     if args.workload in ("tiles_4096", "adjoint_512", "tiles_256_adjoint"):
         if rank == 0:
             fn = {"tiles_4096": run_tiles, "adjoint_512": run_adjoint,
@@ -652,6 +728,8 @@ def main():
         out["adjoint"] = run_adjoint(max(1, min(args.steps, 3)), 1)
         out["batched_adjoint"] = run_tiles_adjoint(max(1, min(args.steps, 3)), 1)
         out["tick_queue"] = run_tick_queue(max(3, min(args.steps, 10)), 3)
+        out["full_step"] = run_full_step(max(3, min(args.steps, 5)), 1,
+                                         cpu_budget_s=0.0 if args.no_cpu else 10.0)
     if rank == 0:
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(tile, os.cpu_count() or 1)
