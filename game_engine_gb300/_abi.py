@@ -148,6 +148,8 @@ SIGNATURES = {
     "wl_batch_tile_count": (C.c_uint32, [C.c_void_p]),
     "wl_batch_cell_count": (C.c_uint64, [C.c_void_p]),
     "wl_batch_tile_first": (C.c_uint64, [C.c_void_p, C.c_uint32]),
+    "wl_batch_write_tile_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, C.c_size_t,
+                                            *_err]),
     "wl_batch_write_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
     "wl_batch_set_bed": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_double, *_err]),
     "wl_batch_set_manning": (C.c_int, [C.c_void_p, _dp, C.c_size_t, *_err]),

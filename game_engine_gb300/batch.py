@@ -84,6 +84,21 @@ class Batch:
                                                hu.ctypes.data_as(_dp), hv.ctypes.data_as(_dp),
                                                self.cells, self._buf, len(self._buf)))
 
+    def write_tile_state(self, tile, h, hu=None, hv=None):
+        """One tile's state between ticks (its ledger emptied, its records primed); the other
+        tiles are untouched: the tile-start upload of a tile that wakes."""
+        nx, ny = self.sides[tile]
+        n = nx * ny
+        h = np.ascontiguousarray(h, dtype=np.float64)
+        hu = np.ascontiguousarray(np.zeros(n) if hu is None else hu, dtype=np.float64)
+        hv = np.ascontiguousarray(np.zeros(n) if hv is None else hv, dtype=np.float64)
+        if not (h.size == hu.size == hv.size):
+            raise BatchError("water_live: spans of different sizes")
+        self._check(lib().wl_batch_write_tile_state(self._h, int(tile), h.ctypes.data_as(_dp),
+                                                    hu.ctypes.data_as(_dp),
+                                                    hv.ctypes.data_as(_dp), h.size, self._buf,
+                                                    len(self._buf)))
+
     def set_bed(self, bed, datum=0.0):
         b = self._arr(bed)
         self._check(lib().wl_batch_set_bed(self._h, b.ctypes.data_as(_dp), self.cells,

@@ -227,6 +227,18 @@ int wl_batch_write_state(wl_batch* b, const double* h, const double* hu, const d
   return WL_OK;
 }
 
+int wl_batch_write_tile_state(wl_batch* b, uint32_t tile, const double* h, const double* hu,
+                              const double* hv, size_t n, char* err, size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (tile >= b->set.tile_count())
+    return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no such tile");
+  if (n != b->set.cells(tile) || h == nullptr || hu == nullptr || hv == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a state that does not fit the tile");
+  std::string msg;
+  if (!b->set.write_tile(tile, h, hu, hv, &msg)) return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
 int wl_batch_set_bed(wl_batch* b, const double* bed, size_t total, double datum, char* err,
                      size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);

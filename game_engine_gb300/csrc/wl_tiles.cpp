@@ -357,6 +357,22 @@ cudaError_t TileSet::enqueue_prime(cudaStream_t s) {
   return launch_prime(shape_, fixed_, a, s);
 }
 
+cudaError_t TileSet::enqueue_tile_prime(cudaStream_t s, uint32_t tile) {
+  TickArgs a;
+  a.tiles = d_desc_ + tile;
+  a.item_tile = nullptr;
+  a.work = d_work_ + 1 + tile;
+  a.n_items = host_[tile].items;
+  a.max_dt = 0.0f;
+  return launch_prime(shape_, fixed_, a, s);
+}
+
+bool TileSet::write_tile(uint32_t tile, const double* h, const double* hu, const double* hv,
+                         std::string* err) {
+  if (!write_state(tile, h, hu, hv, err)) return false;
+  return check(enqueue_tile_prime(stream_, tile), err, "the tile's prime pass") && wait(err);
+}
+
 cudaError_t TileSet::enqueue_length_pass(cudaStream_t s, uint32_t tile, float max_dt) {
   return launch_length_pass(fixed_, d_desc_, tile, max_dt, s);
 }

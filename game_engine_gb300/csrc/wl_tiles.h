@@ -45,6 +45,8 @@ class TileSet {
   // One tile's own tick (the per-tile-launch form): only that tile's work items.
   cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);
   cudaError_t enqueue_prime(cudaStream_t s);
+  // One tile's records alone (its own items): the other tiles' pending records stay as they are.
+  cudaError_t enqueue_tile_prime(cudaStream_t s, uint32_t tile);
   cudaError_t enqueue_length_pass(cudaStream_t s, uint32_t tile, float max_dt);
 
   // ---- synchronous uploads and read-backs (each waits on the set's stream) -----------------
@@ -64,6 +66,9 @@ class TileSet {
 
   // ---- whole batches: arrays of every tile's cells, tile after tile in index order ---------
   bool write_all(const double* h, const double* hu, const double* hv, std::string* err);
+  // One tile's state (its ledger emptied, its records primed); the other tiles are untouched.
+  bool write_tile(uint32_t tile, const double* h, const double* hu, const double* hv,
+                  std::string* err);
   bool set_plane_all(int which, const double* v, double datum, std::string* err);
   bool set_flags_all(uint32_t flags_set, uint32_t flags_clear, uint32_t source_every,
                      bool reset_phase, std::string* err);

@@ -213,6 +213,12 @@ uint64_t wl_batch_tile_first(const wl_batch* batch, uint32_t tile);
 /* write_state / set_bed / set_manning / set_source of every tile at once (total = all cells). */
 int wl_batch_write_state(wl_batch* batch, const double* depth, const double* momentum_x,
                          const double* momentum_y, size_t total, char* err, size_t err_len);
+/* write_state of one tile between ticks (n = its cells): its ledger emptied and its records
+ * primed, every other tile's state, records and ledger untouched. The tile-start upload of a tile
+ * that wakes from the baked solve (ADR-0080:30). */
+int wl_batch_write_tile_state(wl_batch* batch, uint32_t tile, const double* depth,
+                              const double* momentum_x, const double* momentum_y, size_t n,
+                              char* err, size_t err_len);
 int wl_batch_set_bed(wl_batch* batch, const double* bed_m, size_t total, double datum_m, char* err,
                      size_t err_len);
 int wl_batch_set_manning(wl_batch* batch, const double* manning, size_t total, char* err,

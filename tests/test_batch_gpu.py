@@ -121,3 +121,40 @@ def test_tiles_configuration_sample(gpu):
     for k in range(0, 48, 5):
         r = oracle_tile(tiles[k], 0, 200, 0.01, source=False)
         assert int(hashes[k]) == r.state_hash(), f"tile {k} {sides[k]}"
+
+
+@pytest.mark.parametrize("rows", [16, 1])
+def test_one_tile_wakes_with_a_new_state(gpu, rows):
+    """A tile's state written between ticks (the tile-start upload of a tile waking from the baked
+    solve): that tile equals an oracle written at the same tick, and every other tile, its
+    pending records and its ledger included, equals its oracle as if nothing happened."""
+    tiles, sides, edges = mixed_tiles()
+    b = Batch(sides, open_edges=edges)
+    b.set_tuning(rows, 0)
+    load(b, tiles)
+    b.run_ticks(11, 0.02)
+    wake = 2
+    nx, ny = sides[wake]
+    x, y = np.meshgrid(np.arange(nx), np.arange(ny))
+    h_new = 0.5 + 0.3 * ((x + 2 * y) % 7 == 0).ravel()
+    hu_new = np.full(nx * ny, 0.05)
+    b.write_tile_state(wake, h_new, hu_new, np.zeros(nx * ny))
+    b.run_ticks(13, 0.02)
+    ledgers = b.ledgers()
+    for k, t in enumerate(tiles):
+        r = oracle.RefStep(oracle.Grid(t.nx, t.ny, t.cell_m, open_edges=edges[k]))
+        r.set_bed(t.bed)
+        r.set_source(t.source)
+        r.write_state(t.h, t.hu, t.hv)
+        r.run_steps(11, 0.02)
+        if k == wake:
+            r.write_state(h_new, hu_new, np.zeros(nx * ny))
+        r.run_steps(13, 0.02)
+        got, want = b.read_tile_bits(k), r.read_state_bits()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"tile {k}"
+        led = r.read_ledger()
+        for key in ("source_m3", "open_edge_out_m3", "roundoff_m3", "time_s", "steps"):
+            assert ledgers[k][key] == led[key], (k, key)
+    with pytest.raises(Exception):
+        b.write_tile_state(wake, np.zeros(3))  # a state that does not fit the tile
+    b.close()
