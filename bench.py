@@ -531,30 +531,14 @@ def run_tick_queue(steps: int, warmup: int, sides=(256, 2048), frame_slots: int 
     return out
 
 
-def full_step_workload(side: int = 2048):
-    """The complete FP64 step's workload: the throughput tile's terrain and depth with every input
-    on: Manning's n 0.03, the rain, a ground store (Green-Ampt K 5e-6 m/s, suction 0.08 m,
-    capacity 0.1 m), a foam made by the dissipation (decay 30 s) and a settling sediment."""
-    from game_engine_gb300 import workloads
-    t = workloads.plain_2048(side)
-    n = t.cells
-    config = dict(nx=t.nx, ny=t.ny, cell_m=t.cell_m, carried=[(30.0, 1e-4, 0.05), (0.0, 0.0, 0.0)])
-    fields = dict(depth=t.h, momentum_x=t.hu, momentum_y=t.hv, ground=np.zeros(n),
-                  carried=np.concatenate([np.zeros(n), 0.01 * t.h]))
-    inputs = dict(bed=t.bed, manning=np.full(n, 0.03), source=t.source,
-                  ground_k=np.full(n, 5e-6), ground_s=np.full(n, 0.08), ground_cap=np.full(n, 0.1),
-                  carried_source=[None, None], carried_exchange=[None, np.full(n, -1e-6)])
-    return t, config, fields, inputs
-
-
 def run_full_step(steps: int, warmup: int, side: int = 2048, ticks: int = 20, cpu_budget_s=10.0):
     """The complete FP64 step (water_state::Solver with every input) on the device: seconds a step
     and cell-updates/s over `ticks` steps of max_dt 0.01 from the same state, against the oracle's
     restatement of the reference's CPU step on one host core, a bounded sample of steps."""
     import torch
-    from game_engine_gb300 import water_state as ws
+    from game_engine_gb300 import water_state as ws, workloads
     dev_index = int(os.environ.get("LOCAL_RANK", "0"))
-    t, config, fields, inputs = full_step_workload(side)
+    t, config, fields, inputs = workloads.full_step(side)
     s = ws.Solver(ws.Config(config["nx"], config["ny"], config["cell_m"], carried=config["carried"],
                             device=dev_index))
     for name, v in fields.items():

@@ -69,7 +69,7 @@ class Tuning(C.Structure):
 class Event(C.Structure):
     """wl_event: a rectangle of one plane a queued tick replaces."""
     _fields_ = [("kind", C.c_uint32), ("x0", C.c_uint32), ("y0", C.c_uint32), ("w", C.c_uint32),
-                ("h", C.c_uint32)]
+                ("h", C.c_uint32), ("tile", C.c_uint32)]
 
 
 class Landed(C.Structure):
@@ -188,6 +188,8 @@ SIGNATURES = {
     "wl_queue_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                   C.POINTER(C.c_void_p), *_err]),
     "wl_queue_destroy": (None, [C.c_void_p]),
+    "wl_batch_queue_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                        C.POINTER(C.c_void_p), *_err]),
     "wl_queue_push": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.POINTER(Event), C.c_uint32,
                                 _fp, C.c_size_t, *_err]),
     "wl_queue_enqueue_slots": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32]),

@@ -27,10 +27,6 @@ struct wl_step {
   wl_queue* queue = nullptr;  // the tick queue attached, which owns the step's clock
 };
 
-struct wl_queue {
-  wl_step* step = nullptr;  // null once the step was destroyed
-  wlc::TickQueue q;
-};
 
 // The mirrored structs keep the reference's sizes and offsets (water_live_tests.cpp:22-36,
 // size_table.cpp:8-10).
@@ -153,7 +149,7 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
 void wl_destroy(wl_step* step) {
   if (step != nullptr && step->queue != nullptr) {
     step->queue->q.destroy();
-    step->queue->step = nullptr;
+    step->queue->owner = nullptr;
   }
   delete step;
 }
@@ -437,7 +433,7 @@ int wl_queue_create(wl_step* step, uint32_t records, uint32_t arena_values, uint
     const int code = msg.find("holds 1 to 64") != std::string::npos ? WL_ERR_ARGUMENT : WL_ERR_CUDA;
     return fail(err, err_len, code, msg);
   }
-  q->step = step;
+  q->owner = &step->queue;
   step->queue = q;
   *out = q;
   return WL_OK;
@@ -445,9 +441,9 @@ int wl_queue_create(wl_step* step, uint32_t records, uint32_t arena_values, uint
 
 void wl_queue_destroy(wl_queue* queue) {
   if (queue == nullptr) return;
-  if (queue->step != nullptr) {
+  if (queue->owner != nullptr) {
     queue->q.destroy();
-    queue->step->queue = nullptr;
+    *queue->owner = nullptr;
   }
   delete queue;
 }
@@ -455,7 +451,7 @@ void wl_queue_destroy(wl_queue* queue) {
 int wl_queue_push(wl_queue* queue, uint32_t tick, float length_s, const wl_event* events,
                   uint32_t n_events, const float* values, size_t n_values, char* err,
                   size_t err_len) {
-  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+  if (queue == nullptr || queue->owner == nullptr || !queue->q.valid())
     return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
   std::string msg;
   const int rc = queue->q.push(tick, length_s, events, n_events, values, n_values, &msg);
@@ -463,29 +459,27 @@ int wl_queue_push(wl_queue* queue, uint32_t tick, float length_s, const wl_event
 }
 
 int wl_queue_enqueue_slots(wl_queue* queue, wl_stream stream, uint32_t slots) {
-  if (queue == nullptr || queue->step == nullptr || !queue->q.valid()) return WL_ERR_INVALID;
-  wl_step* s = queue->step;
-  cudaStream_t st = stream == nullptr ? s->set.stream() : reinterpret_cast<cudaStream_t>(stream);
-  if (cudaSetDevice(s->set.device()) != cudaSuccess) return WL_ERR_CUDA;
+  if (queue == nullptr || queue->owner == nullptr || !queue->q.valid()) return WL_ERR_INVALID;
+  cudaStream_t st = stream == nullptr ? queue->q.stream() : reinterpret_cast<cudaStream_t>(stream);
+  if (cudaSetDevice(queue->q.device()) != cudaSuccess) return WL_ERR_CUDA;
   return queue->q.enqueue(st, slots) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
 }
 
 int wl_queue_run_slots(wl_queue* queue, uint32_t slots, char* err, size_t err_len) {
-  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+  if (queue == nullptr || queue->owner == nullptr || !queue->q.valid())
     return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
-  wl_step* s = queue->step;
-  if (cudaSetDevice(s->set.device()) != cudaSuccess)
+  if (cudaSetDevice(queue->q.device()) != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
-  const cudaError_t e = queue->q.enqueue(s->set.stream(), slots);
+  const cudaError_t e = queue->q.enqueue(queue->q.stream(), slots);
   if (e != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, std::string("water_live: the slots: ") + cudaGetErrorString(e));
   std::string msg;
-  if (!s->set.wait(&msg)) return cuda_fail(err, err_len, msg);
+  if (!queue->q.wait(&msg)) return cuda_fail(err, err_len, msg);
   return WL_OK;
 }
 
 int wl_queue_status_read(wl_queue* queue, wl_queue_status* out, char* err, size_t err_len) {
-  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+  if (queue == nullptr || queue->owner == nullptr || !queue->q.valid())
     return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
   if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no status to fill");
   wlc::QueueCtl c;
@@ -502,7 +496,7 @@ int wl_queue_status_read(wl_queue* queue, wl_queue_status* out, char* err, size_
 
 int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_landed* out,
                          char* err, size_t err_len) {
-  if (queue == nullptr || queue->step == nullptr || !queue->q.valid())
+  if (queue == nullptr || queue->owner == nullptr || !queue->q.valid())
     return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
   std::string msg;
   if (!queue->q.read_landed(first, count, out, &msg)) {
@@ -515,7 +509,7 @@ int wl_queue_read_landed(wl_queue* queue, uint32_t first, uint32_t count, wl_lan
 uint32_t wl_queue_launches_per_slot(void) { return 2u; }
 
 uint64_t wl_queue_device_bytes(const wl_queue* queue) {
-  return queue != nullptr && queue->step != nullptr ? queue->q.device_bytes() : 0u;
+  return queue != nullptr && queue->owner != nullptr ? queue->q.device_bytes() : 0u;
 }
 
 }  // extern "C"

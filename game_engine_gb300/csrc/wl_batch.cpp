@@ -4,6 +4,7 @@
 #include "wlcuda.h"
 
 #include "wl_adjoint.h"
+#include "wl_queue.h"
 #include "wl_tiles.h"
 
 #include <algorithm>
@@ -32,6 +33,7 @@ struct wl_batch {
   uint32_t flags = 0;  // the batch's Manning / source / compensate flags
   uint32_t source_every = 1;
   wl_tuning tuning{};
+  wl_queue* queue = nullptr;  // a tick queue attached owns the tiles' clocks
   // The captured graph of `graph_ticks` ticks and what it was captured for.
   cudaGraphExec_t graph = nullptr;
   uint32_t graph_ticks = 0;
@@ -66,6 +68,7 @@ int cuda_fail(char* err, size_t len, const std::string& msg) {
 
 bool valid(const wl_batch* b) { return b != nullptr && b->set.valid(); }
 const char* k_no_device = "water_live: no device";
+const char* k_queued = "water_live: the batch's tick queue owns its clocks (destroy the queue first)";
 
 // block_rows: the rows one warp marches (4: the 32 x 16 items split over a CTA's four warps; 1: the
 // 32 x 16 items in three phases, no march).
@@ -207,7 +210,13 @@ int wl_batch_create(const wl_config* common, const wl_options* options, const wl
   return WL_OK;
 }
 
-void wl_batch_destroy(wl_batch* b) { delete b; }
+void wl_batch_destroy(wl_batch* b) {
+  if (b != nullptr && b->queue != nullptr) {
+    b->queue->q.destroy();
+    b->queue->owner = nullptr;
+  }
+  delete b;
+}
 
 uint32_t wl_batch_tile_count(const wl_batch* b) { return valid(b) ? b->set.tile_count() : 0u; }
 
@@ -220,6 +229,7 @@ uint64_t wl_batch_tile_first(const wl_batch* b, uint32_t tile) {
 int wl_batch_write_state(wl_batch* b, const double* h, const double* hu, const double* hv,
                          size_t total, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (total != b->set.total_cells() || h == nullptr || hu == nullptr || hv == nullptr)
     return fail(err, err_len, WL_ERR_SIZE, "water_live: states that do not fit the tiles");
   std::string msg;
@@ -230,6 +240,7 @@ int wl_batch_write_state(wl_batch* b, const double* h, const double* hu, const d
 int wl_batch_write_tile_state(wl_batch* b, uint32_t tile, const double* h, const double* hu,
                               const double* hv, size_t n, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (tile >= b->set.tile_count())
     return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no such tile");
   if (n != b->set.cells(tile) || h == nullptr || hu == nullptr || hv == nullptr)
@@ -273,6 +284,9 @@ int wl_batch_set_manning(wl_batch* b, const double* manning, size_t total, char*
 int wl_batch_set_source(wl_batch* b, const double* source, size_t total, uint32_t every,
                         int compensate, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr && every > 1)
+    return fail(err, err_len, WL_ERR_REFUSED,
+                "water_live: a batch with a tick queue refuses a coarser source clock");
   b->source_every = every == 0 ? 1 : every;
   const uint32_t comp = compensate ? WL_FLAG_COMPENSATE : 0u;
   std::string msg;
@@ -295,6 +309,7 @@ int wl_batch_set_source(wl_batch* b, const double* source, size_t total, uint32_
 
 int wl_batch_enqueue_ticks(wl_batch* b, wl_stream stream, uint32_t count, float max_dt) {
   if (!valid(b)) return WL_ERR_INVALID;
+  if (b->queue != nullptr) return WL_ERR_REFUSED;
   if (cudaSetDevice(b->set.device()) != cudaSuccess) return WL_ERR_CUDA;
   cudaStream_t st = stream == nullptr ? b->set.stream() : reinterpret_cast<cudaStream_t>(stream);
   return b->set.enqueue_ticks(st, count, max_dt) == cudaSuccess ? WL_OK : WL_ERR_CUDA;
@@ -303,6 +318,7 @@ int wl_batch_enqueue_ticks(wl_batch* b, wl_stream stream, uint32_t count, float 
 int wl_batch_run_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph, char* err,
                        size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (cudaSetDevice(b->set.device()) != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
   cudaStream_t st = b->set.stream();
@@ -346,6 +362,7 @@ int wl_batch_run_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph,
 
 int wl_batch_enqueue_tile_tick(wl_batch* b, wl_stream stream, uint32_t tile, float max_dt) {
   if (!valid(b)) return WL_ERR_INVALID;
+  if (b->queue != nullptr) return WL_ERR_REFUSED;
   if (tile >= b->set.tile_count()) return WL_ERR_ARGUMENT;
   if (cudaSetDevice(b->set.device()) != cudaSuccess) return WL_ERR_CUDA;
   cudaStream_t st = stream == nullptr ? b->set.stream() : reinterpret_cast<cudaStream_t>(stream);
@@ -355,6 +372,7 @@ int wl_batch_enqueue_tile_tick(wl_batch* b, wl_stream stream, uint32_t tile, flo
 int wl_batch_run_tile_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph,
                             uint32_t streams, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (cudaSetDevice(b->set.device()) != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
   cudaStream_t st = b->set.stream();
@@ -506,6 +524,7 @@ int wl_batch_read_ledgers(wl_batch* b, wl_ledger* out, uint32_t count, char* err
 
 int wl_batch_set_tuning(wl_batch* b, const wl_tuning* t, char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (t == nullptr ||
       (t->block_rows != 1 && t->block_rows != 4 && t->block_rows != 16 && t->block_rows != 32 &&
        t->block_rows != 64) ||
@@ -528,6 +547,7 @@ int wl_batch_get_tuning(const wl_batch* b, wl_tuning* out) {
 int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning* chosen,
                       char* err, size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr) return fail(err, err_len, WL_ERR_REFUSED, k_queued);
   if (cudaSetDevice(b->set.device()) != cudaSuccess)
     return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
   int sms = 0;
@@ -585,6 +605,30 @@ int wl_batch_adjoint_create(wl_batch* batch, uint32_t ticks, uint32_t every,
     return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no probes or targets");
   return wl_adjoint_create_over(&batch->set, ticks, every, probe_first, probes, targets, out, err,
                                 err_len);
+}
+
+int wl_batch_queue_create(wl_batch* b, uint32_t records, uint32_t arena_values,
+                          uint32_t max_events, wl_queue** out, char* err, size_t err_len) {
+  if (out == nullptr) return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: no handle to fill");
+  *out = nullptr;
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (b->queue != nullptr)
+    return fail(err, err_len, WL_ERR_REFUSED, "water_live: the batch has a tick queue already");
+  if ((b->flags & WL_FLAG_SOURCE) != 0u && b->source_every > 1)
+    return fail(err, err_len, WL_ERR_REFUSED,
+                "water_live: a tick queue refuses a source on a coarser clock (set_source every > 1)");
+  auto* q = new (std::nothrow) wl_queue;
+  if (q == nullptr) return fail(err, err_len, WL_ERR_ALLOC, "water_live: host memory");
+  std::string msg;
+  if (!q->q.create(&b->set, records, arena_values, max_events, &msg)) {
+    delete q;
+    const int code = msg.find("holds 1 to 64") != std::string::npos ? WL_ERR_ARGUMENT : WL_ERR_CUDA;
+    return fail(err, err_len, code, msg);
+  }
+  q->owner = &b->queue;
+  b->queue = q;
+  *out = q;
+  return WL_OK;
 }
 
 }  // extern "C"

@@ -649,6 +649,8 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
     const float pa = __uint_as_float(ctl->max_a[it.rec]);
     const float pb = __uint_as_float(ctl->max_b[it.rec]);
     it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[it.rec].remaining_s);
+    // A tick queue's slot: a tile with no time left has landed and waits for the others.
+    if (a.go != nullptr && !(ctl->ledger[it.rec].remaining_s > 0.0f)) continue;
     const bool src = (T.flags & kFlagSource) != 0u;
     const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     it.apply_source = on ? 1u : 0u;
@@ -717,6 +719,10 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
     const float pa = __uint_as_float(ctl->max_a[it.rec]);
     const float pb = __uint_as_float(ctl->max_b[it.rec]);
     it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[it.rec].remaining_s);
+    if (a.go != nullptr && !(ctl->ledger[it.rec].remaining_s > 0.0f)) {  // a landed tile
+      __syncthreads();
+      continue;
+    }
     const bool src = (T.flags & kFlagSource) != 0u;
     const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     it.apply_source = on ? 1u : 0u;
@@ -802,6 +808,10 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
     const float pa = __uint_as_float(ctl->max_a[rec]), pb = __uint_as_float(ctl->max_b[rec]);
     const float dt =
         choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[rec].remaining_s);
+    if (a.go != nullptr && !(ctl->ledger[rec].remaining_s > 0.0f)) {  // a landed tile
+      __syncthreads();
+      continue;
+    }
     const bool src_flag = (T.flags & kFlagSource) != 0u;
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;

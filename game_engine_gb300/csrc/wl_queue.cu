@@ -29,7 +29,8 @@ namespace {
 constexpr uint32_t kMaxRecords = 64;  // water_live.md:84
 constexpr int kApplyThreads = 1024;
 
-// The tick in flight's read-back record, and the queue free for the next.
+// The tick in flight's read-back record (tile 0's ledger time and step count), and the queue
+// free for the next.
 __device__ void land(QueueCtl* q, const LedgerBits& l, wl_landed* landed, uint32_t records) {
   wl_landed r;
   r.tick = q->tick;
@@ -45,77 +46,108 @@ __device__ void land(QueueCtl* q, const LedgerBits& l, wl_landed* landed, uint32
   q->active = 0u;
 }
 
-// The last slot's effects: the release of the events its apply read, its sub-step (the ledger's
-// step count moved) and a landing (a tick in flight with no time left).
-__device__ void settle(QueueCtl* q, const TileCtl* ctl, wl_landed* landed, uint32_t records) {
-  const LedgerBits& l = ctl->ledger[ctl->rec];
-  if (q->apply != 0u) {
-    q->events_done = q->first_event + q->events;
-    q->values_done = q->values_end;
-    q->apply = 0u;
-  }
-  if (l.steps != q->seen_steps) {
-    q->seen_steps = l.steps;
-    q->substeps += 1u;
-    q->shortest = fminf(q->shortest, l.dt);
-    q->longest = fmaxf(q->longest, l.dt);
-  }
-  if (q->active != 0u && !(l.remaining_s > 0.0f)) land(q, l, landed, records);
+__device__ __forceinline__ const LedgerBits& current(const TileDesc& T) {
+  return T.ctl->ledger[T.ctl->rec];
 }
 
-// Thread 0's part of a slot: the settle and the begin.
-__device__ void begin(QueueCtl* q, const QueueRecord* ring, TileCtl* ctl, wl_landed* landed,
-                      uint32_t records, int may_begin) {
-  volatile QueueCtl* vq = q;
-  settle(q, ctl, landed, records);
-  const uint32_t head = vq->head;  // the host's word
-  if (may_begin != 0 && q->active == 0u && q->begun != head) {
-    const QueueRecord r = ring[q->begun % records];
-    q->begun += 1u;
-    q->tick = r.tick;
-    q->events = r.events;
-    q->first_event = r.first_event;
-    q->values_end = r.values_end;
-    q->substeps = 0u;
-    q->shortest = __int_as_float(0x7f800000);
-    q->longest = 0.0f;
-    q->apply = r.events != 0u ? 1u : 0u;
-    q->active = 1u;
-    LedgerBits& l = ctl->ledger[ctl->rec];
-    l.remaining_s = r.length_s > 0.0f ? r.length_s : 0.0f;
-    // A tick of no length lands now; its events are applied later in this slot all the same.
-    if (!(r.length_s > 0.0f)) land(q, l, landed, records);
-  }
-  q->go = q->active;
-}
-
-// A slot's first launch: thread 0's begin, then the begun tick's events by the whole CTA, one
-// after another (a later event over the same cells wins). The host checked every rectangle
-// against the grid and every plane's presence when it pushed them. With may_begin 0 it only
-// settles (the call's last launch, so a read-back after it sees the last slot's effects).
+// A slot's first launch, one CTA over the queue's tiles (a step is a set of one):
+//   1. the last slot's effects: a tile whose step count moved took a sub-step (its length into
+//      the tick's shortest and longest), the events the last slot applied are released, and the
+//      tick in flight lands when no tile has time left;
+//   2. thread 0's begin: when no tick is in flight and one is queued, every tile's time left
+//      becomes its length;
+//   3. the begun tick's events into the planes, one after another (a later event over the same
+//      cells wins). The host checked every rectangle against its tile and every plane's presence.
+// With may_begin 0 it only settles (the call's last launch, so a read-back after it sees the last
+// slot's effects).
 __global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
-    QueueCtl* q, const QueueRecord* ring, TileCtl* ctl, wl_landed* landed, uint32_t records,
-    int may_begin, const QueueEvent* events, uint32_t max_events, const float* arena,
-    uint32_t arena_values, const TileDesc* T) {
-  __shared__ uint32_t s_apply;
-  if (threadIdx.x == 0) {
-    begin(q, ring, ctl, landed, records, may_begin);
+    QueueCtl* q, const QueueRecord* ring, uint32_t records, wl_landed* landed,
+    const TileDesc* tiles, uint32_t n_tiles, uint32_t* seen, int may_begin,
+    const QueueEvent* events, uint32_t max_events, const float* arena, uint32_t arena_values) {
+  __shared__ uint32_t s_left, s_stepped, s_min, s_max, s_begin, s_apply;
+  __shared__ float s_len;
+  const uint32_t t = threadIdx.x;
+  if (t == 0) {
+    s_left = 0u;
+    s_stepped = 0u;
+    s_min = 0x7f800000u;  // +inf: lengths are >= 0, so their bits order as they do
+    s_max = 0u;
+  }
+  __syncthreads();
+  uint32_t left = 0u, stepped = 0u, lo = 0x7f800000u, hi = 0u;
+  for (uint32_t k = t; k < n_tiles; k += blockDim.x) {
+    const LedgerBits& l = current(tiles[k]);
+    if (l.steps != seen[k]) {
+      seen[k] = l.steps;
+      stepped = 1u;
+      lo = min(lo, __float_as_uint(l.dt));
+      hi = max(hi, __float_as_uint(l.dt));
+    }
+    if (l.remaining_s > 0.0f) left = 1u;
+  }
+  if (left != 0u) atomicOr(&s_left, 1u);
+  if (stepped != 0u) {
+    atomicOr(&s_stepped, 1u);
+    atomicMin(&s_min, lo);
+    atomicMax(&s_max, hi);
+  }
+  __syncthreads();
+  if (t == 0) {
+    if (q->apply != 0u) {
+      q->events_done = q->first_event + q->events;
+      q->values_done = q->values_end;
+      q->apply = 0u;
+    }
+    if (s_stepped != 0u) {
+      q->substeps += 1u;
+      q->shortest = fminf(q->shortest, __uint_as_float(s_min));
+      q->longest = fmaxf(q->longest, __uint_as_float(s_max));
+    }
+    if (q->active != 0u && s_left == 0u) land(q, current(tiles[0]), landed, records);
+    s_begin = 0u;
+    const uint32_t head = *static_cast<volatile uint32_t*>(&q->head);  // the host's word
+    if (may_begin != 0 && q->active == 0u && q->begun != head) {
+      const QueueRecord r = ring[q->begun % records];
+      q->begun += 1u;
+      q->tick = r.tick;
+      q->events = r.events;
+      q->first_event = r.first_event;
+      q->values_end = r.values_end;
+      q->substeps = 0u;
+      q->shortest = __int_as_float(0x7f800000);
+      q->longest = 0.0f;
+      q->apply = r.events != 0u ? 1u : 0u;
+      q->active = 1u;
+      s_begin = 1u;
+      s_len = r.length_s > 0.0f ? r.length_s : 0.0f;
+    }
     s_apply = q->apply;
   }
   __syncthreads();
+  if (s_begin != 0u) {
+    for (uint32_t k = t; k < n_tiles; k += blockDim.x) {
+      TileCtl* c = tiles[k].ctl;
+      c->ledger[c->rec].remaining_s = s_len;
+    }
+    __syncthreads();
+    // A tick of no length lands now; its events are applied below all the same.
+    if (t == 0 && !(s_len > 0.0f)) land(q, current(tiles[0]), landed, records);
+  }
+  if (t == 0) q->go = q->active;
   if (s_apply == 0u) return;
   const uint32_t n = q->events;
   const uint64_t first = q->first_event;
   for (uint32_t e = 0; e < n; ++e) {
     const QueueEvent ev = events[(first + e) % max_events];
-    float* dst = const_cast<float*>(ev.kind == WL_EVENT_BED      ? T->bed
-                                    : ev.kind == WL_EVENT_SOURCE ? T->source
-                                                                 : T->manning);
+    const TileDesc& T = tiles[ev.tile];
+    float* dst = const_cast<float*>(ev.kind == WL_EVENT_BED      ? T.bed
+                                    : ev.kind == WL_EVENT_SOURCE ? T.source
+                                                                 : T.manning);
     const float* src = arena + ev.value_first % arena_values;
     const uint32_t count = ev.w * ev.h;
-    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
+    for (uint32_t k = t; k < count; k += blockDim.x) {
       const uint32_t y = k / ev.w, x = k - y * ev.w;
-      dst[size_t(ev.y0 + y) * T->nx + ev.x0 + x] = src[k];
+      dst[size_t(ev.y0 + y) * T.nx + ev.x0 + x] = src[k];
     }
     __syncthreads();
   }
@@ -148,7 +180,9 @@ bool TickQueue::create(TileSet* set, uint32_t records, uint32_t arena_values, ui
   const size_t b_events = align_up(size_t(max_events) * sizeof(QueueEvent));
   const size_t b_landed = align_up(size_t(records) * sizeof(wl_landed));
   const size_t b_arena = align_up(size_t(arena_values) * sizeof(float));
-  bytes_ = b_ctl + b_ring + b_events + b_landed + b_arena;
+  const uint32_t n_tiles = set->tile_count();
+  const size_t b_seen = align_up(size_t(n_tiles) * sizeof(uint32_t));
+  bytes_ = b_ctl + b_ring + b_events + b_landed + b_arena + b_seen;
   if (!ok(cudaMalloc(reinterpret_cast<void**>(&base_), bytes_), err, "cudaMalloc of the queue")) {
     base_ = nullptr;
     return false;
@@ -158,6 +192,8 @@ bool TickQueue::create(TileSet* set, uint32_t records, uint32_t arena_values, ui
   d_events_ = reinterpret_cast<QueueEvent*>(base_ + b_ctl + b_ring);
   d_landed_ = reinterpret_cast<wl_landed*>(base_ + b_ctl + b_ring + b_events);
   d_arena_ = reinterpret_cast<float*>(base_ + b_ctl + b_ring + b_events + b_landed);
+  d_seen_ = reinterpret_cast<uint32_t*>(base_ + b_ctl + b_ring + b_events + b_landed + b_arena);
+  tiles_ = n_tiles;
   set_ = set;
   records_ = records;
   max_events_ = max_events;
@@ -165,18 +201,22 @@ bool TickQueue::create(TileSet* set, uint32_t records, uint32_t arena_values, ui
   pushed_ = 0;
   events_pushed_ = 0;
   values_pushed_ = 0;
-  // The settle counts sub-steps from the ledger's step count as it stands now.
-  TileCtl c;
-  if (!set->read_ctl(0, c, err)) {
+  // The settle counts sub-steps from each tile's step count as it stands now.
+  std::vector<TileCtl> ctl(n_tiles);
+  if (!set->read_all_ctl(ctl.data(), err)) {
     destroy();
     return false;
   }
+  std::vector<uint32_t> seen(n_tiles);
+  for (uint32_t k = 0; k < n_tiles; ++k) seen[k] = ctl[k].ledger[ctl[k].rec & 1u].steps;
   QueueCtl q;
   std::memset(&q, 0, sizeof q);
-  q.seen_steps = c.ledger[c.rec & 1u].steps;
   if (!ok(cudaMemsetAsync(base_, 0, bytes_, set->stream()), err, "cudaMemset of the queue") ||
       !ok(cudaMemcpyAsync(d_ctl_, &q, sizeof q, cudaMemcpyHostToDevice, set->stream()), err,
           "upload of the queue") ||
+      !ok(cudaMemcpyAsync(d_seen_, seen.data(), n_tiles * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice, set->stream()),
+          err, "upload of the step counts") ||
       !set->wait(err)) {
     destroy();
     return false;
@@ -189,9 +229,10 @@ void TickQueue::destroy() {
     if (set_ != nullptr && set_->valid()) {
       cudaSetDevice(set_->device());
       cudaStreamSynchronize(set_->stream());
-      // The step's clock back to the free-running form: no time to count down.
+      // Each tile's clock back to the free-running form: no time to count down.
       std::string ignored;
-      set_->set_remaining(0, std::numeric_limits<float>::infinity(), &ignored);
+      for (uint32_t k = 0; k < tiles_; ++k)
+        set_->set_remaining(k, std::numeric_limits<float>::infinity(), &ignored);
     }
     cudaFree(base_);
   }
@@ -226,10 +267,14 @@ int TickQueue::push(uint32_t tick, float length_s, const wl_event* events, uint3
     if (err) *err = "water_live: no events";
     return WL_ERR_ARGUMENT;
   }
-  const TileDesc& d = set_->desc(0);
   uint64_t need = 0;
   for (uint32_t e = 0; e < n_events; ++e) {
     const wl_event& ev = events[e];
+    if (ev.tile >= tiles_) {
+      if (err) *err = "water_live: an event's tile is not in the queue's set";
+      return WL_ERR_ARGUMENT;
+    }
+    const TileDesc& d = set_->desc(ev.tile);
     const bool plane = ev.kind == WL_EVENT_BED ||
                        (ev.kind == WL_EVENT_SOURCE && d.source != nullptr &&
                         (d.flags & kFlagSource) != 0u) ||
@@ -270,7 +315,7 @@ int TickQueue::push(uint32_t tick, float length_s, const wl_event* events, uint3
   uint64_t at = base;
   for (uint32_t e = 0; e < n_events; ++e) {
     const wl_event& ev = events[e];
-    dev[e] = QueueEvent{ev.kind, ev.x0, ev.y0, ev.w, ev.h, 0u, at};
+    dev[e] = QueueEvent{ev.kind, ev.x0, ev.y0, ev.w, ev.h, ev.tile, at};
     at += uint64_t(ev.w) * ev.h;
   }
   // Events and values first, the record, then `head`: a slot that sees the new head finds them.
@@ -304,20 +349,20 @@ int TickQueue::push(uint32_t tick, float length_s, const wl_event* events, uint3
 
 cudaError_t TickQueue::enqueue(cudaStream_t s, uint32_t slots) {
   if (!valid()) return cudaErrorInvalidValue;
-  const TileDesc& d = set_->desc(0);
   const float inf = std::numeric_limits<float>::infinity();
+  const TileDesc* tiles = set_->device_descs();
   for (uint32_t k = 0; k < slots; ++k) {
-    queue_slot_kernel<<<1, kApplyThreads, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 1,
-                                                   d_events_, max_events_, d_arena_, arena_,
-                                                   set_->device_descs());
+    queue_slot_kernel<<<1, kApplyThreads, 0, s>>>(d_ctl_, d_ring_, records_, d_landed_, tiles,
+                                                   tiles_, d_seen_, 1, d_events_, max_events_,
+                                                   d_arena_, arena_);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = set_->enqueue_ticks(s, 1, inf, &d_ctl_->go);
     if (e != cudaSuccess) return e;
   }
   // The last slot's effects, so a read-back after the call sees them.
-  queue_slot_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, d.ctl, d_landed_, records_, 0, d_events_,
-                                     max_events_, d_arena_, arena_, set_->device_descs());
+  queue_slot_kernel<<<1, 32, 0, s>>>(d_ctl_, d_ring_, records_, d_landed_, tiles, tiles_, d_seen_,
+                                     0, d_events_, max_events_, d_arena_, arena_);
   return cudaGetLastError();
 }
 

@@ -25,9 +25,9 @@ struct QueueRecord {
 };
 static_assert(sizeof(QueueRecord) == 32, "QueueRecord layout");
 
-// An event as the device holds it: a rectangle of one plane and where its values start.
+// An event as the device holds it: a rectangle of one plane of one tile and where its values start.
 struct QueueEvent {
-  uint32_t kind, x0, y0, w, h, pad;
+  uint32_t kind, x0, y0, w, h, tile;
   uint64_t value_first;  // absolute arena index (the host keeps an event's values contiguous)
 };
 static_assert(sizeof(QueueEvent) == 32, "QueueEvent layout");
@@ -41,8 +41,8 @@ struct QueueCtl {
   uint32_t active;      // a begun tick has not landed
   uint32_t go;          // this slot's tick steps
   uint32_t apply;       // this slot's apply writes the begun tick's events
-  uint32_t substeps;    // sub-steps of the tick in flight
-  uint32_t seen_steps;  // the ledger's step count the last settle saw
+  uint32_t substeps;    // slots in which a tile of the tick in flight stepped
+  uint32_t pad;
   float shortest, longest;
   uint32_t tick, events;  // the tick in flight: its number and its event count
   uint64_t first_event;   // its first event
@@ -54,7 +54,7 @@ struct QueueCtl {
 class TickQueue {
  public:
   ~TickQueue() { destroy(); }
-  // Over tile 0 of `set` (a step). records <= 64.
+  // Over every tile of `set` (a step is a set of one tile). records <= 64.
   bool create(TileSet* set, uint32_t records, uint32_t arena_values, uint32_t max_events,
               std::string* err);
   void destroy();
@@ -66,6 +66,9 @@ class TickQueue {
   bool read_ctl(QueueCtl& out, std::string* err);
   bool read_landed(uint32_t first, uint32_t count, wl_landed* out, std::string* err);
   uint64_t device_bytes() const { return bytes_; }
+  cudaStream_t stream() const { return set_ != nullptr ? set_->stream() : nullptr; }
+  int device() const { return set_ != nullptr ? set_->device() : -1; }
+  bool wait(std::string* err) { return set_ != nullptr && set_->wait(err); }
 
  private:
   TileSet* set_ = nullptr;
@@ -76,6 +79,8 @@ class TickQueue {
   QueueEvent* d_events_ = nullptr;
   float* d_arena_ = nullptr;
   wl_landed* d_landed_ = nullptr;
+  uint32_t* d_seen_ = nullptr;  // each tile's step count at the last settle
+  uint32_t tiles_ = 0;
   uint32_t records_ = 0, max_events_ = 0, arena_ = 0;
   uint32_t pushed_ = 0;        // records pushed
   uint64_t events_pushed_ = 0;  // events pushed
@@ -83,3 +88,10 @@ class TickQueue {
 };
 
 }  // namespace wlc
+
+// The C ABI's queue handle (wlcuda.h), over a step's or a batch's tile set. `owner` is the owner's
+// own field that points back at the handle; whichever of the two goes first clears the link.
+struct wl_queue {
+  wlc::TickQueue q;
+  wl_queue** owner = nullptr;
+};

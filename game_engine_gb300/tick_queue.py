@@ -23,26 +23,31 @@ _fp = C.POINTER(C.c_float)
 
 @dataclass
 class Event:
-    """A rectangle of one plane (EVENT_*) replaced by ``values`` (h rows of w, row by row)."""
+    """A rectangle of one plane (EVENT_*) of one tile replaced by ``values`` (h rows of w, row by
+    row); tile 0 for a step's queue."""
     kind: int
     x0: int
     y0: int
     values: np.ndarray  # shape (h, w)
+    tile: int = 0
 
 
 class TickQueue:
-    """The queue of ticks over one ``water_live.DeviceStep``."""
+    """The queue of ticks over one ``water_live.DeviceStep`` or one ``batch.Batch`` (the domain's
+    tiles take every tick together, each by its own sub-steps)."""
 
-    def __init__(self, step, records: int = MAX_RECORDS, arena_values: int = 1 << 16,
+    def __init__(self, owner, records: int = MAX_RECORDS, arena_values: int = 1 << 16,
                  max_events: int = 256):
+        from .batch import Batch
         self.error = ""
         self.last_code = 0
         self._buf = C.create_string_buffer(512)
         self._h = None
-        self._step = step
+        self._owner = owner
         h = C.c_void_p()
-        rc = lib().wl_queue_create(step.handle, int(records), int(arena_values), int(max_events),
-                                   C.byref(h), self._buf, len(self._buf))
+        create = lib().wl_batch_queue_create if isinstance(owner, Batch) else lib().wl_queue_create
+        rc = create(owner.handle, int(records), int(arena_values), int(max_events), C.byref(h),
+                    self._buf, len(self._buf))
         if rc != 0:
             raise RuntimeError(self._buf.value.decode())
         self._h = h
@@ -72,7 +77,7 @@ class TickQueue:
         for k, e in enumerate(events):
             v = np.ascontiguousarray(e.values, dtype=np.float32)
             h, w = v.shape
-            evs[k] = _abi.Event(int(e.kind), int(e.x0), int(e.y0), int(w), int(h))
+            evs[k] = _abi.Event(int(e.kind), int(e.x0), int(e.y0), int(w), int(h), int(e.tile))
             vals.append(v.ravel())
         flat = np.concatenate(vals) if vals else np.zeros(1, np.float32)
         n_values = int(sum(v.size for v in vals))

@@ -160,6 +160,21 @@ def plain_2048(side: int = 2048) -> Tile:
                                "rain 1e-5 m a tick"))
 
 
+def full_step(side: int = 2048):
+    """The complete FP64 step's workload: the throughput tile's terrain and depth with every input
+    on: Manning's n 0.03, the rain, a ground store (Green-Ampt K 5e-6 m/s, suction 0.08 m,
+    capacity 0.1 m), a foam made by the dissipation (decay 30 s) and a settling sediment."""
+    t = plain_2048(side)
+    n = t.cells
+    config = dict(nx=t.nx, ny=t.ny, cell_m=t.cell_m, carried=[(30.0, 1e-4, 0.05), (0.0, 0.0, 0.0)])
+    fields = dict(depth=t.h, momentum_x=t.hu, momentum_y=t.hv, ground=np.zeros(n),
+                  carried=np.concatenate([np.zeros(n), 0.01 * t.h]))
+    inputs = dict(bed=t.bed, manning=np.full(n, 0.03), source=t.source,
+                  ground_k=np.full(n, 5e-6), ground_s=np.full(n, 0.08), ground_cap=np.full(n, 0.1),
+                  carried_source=[None, None], carried_exchange=[None, np.full(n, -1e-6)])
+    return t, config, fields, inputs
+
+
 TILE_SIDES = (64, 96, 128, 192, 256, 384, 512)
 
 

@@ -342,10 +342,12 @@ enum {
   WL_EVENT_MANNING = 2 /* Manning's n over the rectangle; the step must have Manning on */
 };
 
-/* One event: a rectangle of one plane replaced by w * h values, row by row. */
+/* One event: a rectangle of one plane of one tile replaced by w * h values, row by row (tile 0
+ * for a step's queue). */
 typedef struct wl_event {
   uint32_t kind;
   uint32_t x0, y0, w, h;
+  uint32_t tile;
 } wl_event;
 
 /* What a landed tick leaves (water_live.md:94): its number, its sub-steps, its shortest and
@@ -374,6 +376,12 @@ typedef struct wl_queue_status {
  * arena of `arena_values` floats and room for `max_events` events. */
 int wl_queue_create(wl_step* step, uint32_t records, uint32_t arena_values, uint32_t max_events,
                     wl_queue** out, char* err, size_t err_len);
+/* The same over a batch: the domain's tiles take every tick together, each by its own sub-steps
+ * (min(its stable step, its time left)); a tick lands when every tile has; a tile that has landed
+ * waits through the slots the others still take. While attached, the batch refuses its own ticks,
+ * tuning, autotuning and state writes. */
+int wl_batch_queue_create(wl_batch* batch, uint32_t records, uint32_t arena_values,
+                          uint32_t max_events, wl_queue** out, char* err, size_t err_len);
 void wl_queue_destroy(wl_queue* queue);
 /* Queues one tick: its number, its length (s, >= 0) and its events with their values, in order
  * (sum of w * h values). Waits for the copy. WL_ERR_REFUSED when the ring, the event ring or the

@@ -215,3 +215,67 @@ def test_a_new_state_is_refused_while_queued(gpu):
     assert not dev.write_state(np.zeros(n), np.zeros(n), np.zeros(n)) and dev.last_code == 5
     q.close()
     assert dev.write_state(np.zeros(n), np.zeros(n), np.zeros(n)), dev.error
+
+
+@pytest.mark.parametrize("rows", [16, 4, 1])
+def test_a_batch_queue_equals_advance_per_tile(gpu, rows):
+    """A domain of uneven tiles: each queued tick advances every tile by its length, each tile by
+    its own sub-steps, with per-tile events; every tile equals its oracle's advance-per-tick run,
+    and each landing counts the slots of its slowest tile."""
+    from game_engine_gb300.batch import Batch, BatchError
+    from test_batch_gpu import load, mixed_tiles
+    import oracle
+    tiles, sides, edges = mixed_tiles()
+    b = Batch(sides, open_edges=edges)
+    b.set_tuning(rows, 0)
+    load(b, tiles)
+    refs = []
+    for k, t in enumerate(tiles):
+        r = oracle.RefStep(oracle.Grid(t.nx, t.ny, t.cell_m, open_edges=edges[k]))
+        r.set_bed(t.bed)
+        r.set_source(t.source)
+        r.write_state(t.h, t.hu, t.hv)
+        refs.append(r)
+    beds = [np.asarray(t.bed, np.float64).astype(np.float32) for t in tiles]
+    srcs = [np.asarray(t.source, np.float64).astype(np.float32) for t in tiles]
+    plan = []
+    for tick in range(14):
+        events, length = [], TICK
+        if tick == 3:
+            events = [Event(EVENT_BED, 2, 1, np.full((3, 4), 0.9), tile=0),
+                      Event(EVENT_BED, 10, 20, np.full((5, 5), 0.1), tile=2)]
+        if tick == 5:
+            events = [Event(EVENT_SOURCE, 0, 0, np.full((4, 4), 5e-3), tile=1)]
+        if tick == 7:
+            length = 0.0
+            events = [Event(EVENT_BED, 0, 0, np.full((2, 3), 0.5), tile=4)]
+        plan.append((tick, length, events))
+    want = []
+    for tick, length, events in plan:
+        for e in events:
+            v = np.asarray(e.values, np.float32)
+            nx, ny = sides[e.tile]
+            p = (beds if e.kind == EVENT_BED else srcs)[e.tile].reshape(ny, nx)
+            p[e.y0:e.y0 + v.shape[0], e.x0:e.x0 + v.shape[1]] = v
+            if e.kind == EVENT_BED:
+                refs[e.tile].set_bed(beds[e.tile].astype(np.float64))
+            else:
+                refs[e.tile].set_source(srcs[e.tile].astype(np.float64))
+        want.append(max(r.advance(length)[0] for r in refs) if length > 0 else 0)
+    q = TickQueue(b, records=16)
+    for p in plan:
+        assert q.push(*p), q.error
+    with pytest.raises(BatchError):
+        b.run_ticks(1, 0.01)  # the queue owns the clocks
+    device_run(q, len(plan), [2, 5, 1])
+    ledgers = b.ledgers()
+    for k, r in enumerate(refs):
+        got, exp = b.read_tile_bits(k), r.read_state_bits()
+        assert np.array_equal(got.view(np.uint32), exp.view(np.uint32)), f"tile {k} {sides[k]}"
+        led = r.read_ledger()
+        for key in LEDGER_SUMS:
+            assert ledgers[k][key] == led[key], (k, key)
+    assert [x["substeps"] for x in q.landed(0, len(plan))] == want
+    q.close()
+    b.run_ticks(1, 0.01)  # the batch's own ticks again
+    b.close()

@@ -137,3 +137,16 @@ def test_a_larger_grid_with_everything_on(gpu):
     assert ws_cases.run(dev, case) == ws_cases.run(ref, case)
     assert_same(dev, ref, "320x288")
     dev.close()
+
+
+def test_the_benchmark_configuration_first_steps(gpu):
+    """The full_step benchmark's 2048 x 2048 tile with every input on: its first 3 steps against
+    the oracle, byte for byte (the oracle takes about a second a step)."""
+    from game_engine_gb300 import workloads
+    t, config, fields, inputs = workloads.full_step(2048)
+    case = dict(config=dict(config, open_edges=0), fields=fields, inputs=inputs,
+                run=[("step", 0.01)] * 3)
+    dev, ref = device_solver(case), oracle_solver(case)
+    assert ws_cases.run(dev, case) == ws_cases.run(ref, case)
+    assert_same(dev, ref, "2048")
+    dev.close()
