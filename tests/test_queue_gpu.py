@@ -49,7 +49,7 @@ def plan_for(c, n_ticks, seed):
     return plan
 
 
-def oracle_run(ref, c, plan):
+def oracle_run(ref, c, plan, compensate=False):
     """The oracle: each tick's events into its planes, then advance(length). Returns the steps."""
     planes = {EVENT_BED: np.asarray(c["bed"], np.float64).astype(np.float32)}
     if c.get("source") is not None:
@@ -65,7 +65,8 @@ def oracle_run(ref, c, plan):
             p[e.y0:e.y0 + v.shape[0], e.x0:e.x0 + v.shape[1]] = v
         for kind in {e.kind for e in events}:
             wide = planes[kind].astype(np.float64)  # f32 values widen exactly; datum 0
-            {EVENT_BED: lambda: ref.set_bed(wide, 0.0), EVENT_SOURCE: lambda: ref.set_source(wide),
+            {EVENT_BED: lambda: ref.set_bed(wide, 0.0),
+             EVENT_SOURCE: lambda: ref.set_source(wide, 1, compensate),
              EVENT_MANNING: lambda: ref.set_manning(wide)}[kind]()
         steps.append(ref.advance(length)[0] if length > 0 else 0)
     return steps
@@ -279,3 +280,28 @@ def test_a_batch_queue_equals_advance_per_tile(gpu, rows):
     q.close()
     b.run_ticks(1, 0.01)  # the batch's own ticks again
     b.close()
+
+
+@pytest.mark.parametrize("form", ["fixed", "stored_faces", "compensate"])
+def test_queued_ticks_in_the_other_forms(gpu, form):
+    """The fixed arithmetic, the stored-faces form and the compensated source through the queue:
+    the same bytes as the oracle's advance per tick."""
+    c = cases.slope(False)
+    kw = {"fixed": dict(fixed=True), "stored_faces": dict(stored_faces=True),
+          "compensate": dict(compensate=True)}[form]
+    dev, ref = make_pair(c, **kw)
+    n = 10
+    plan = plan_for(c, n, seed=23)
+    if form == "compensate":
+        # a source event resets nothing of the remainder: the oracle's set_source would, so the
+        # plan carries bed events alone
+        plan = [(t, l, [e for e in ev if e.kind == EVENT_BED]) for t, l, ev in plan]
+    oracle_run_kw = dict(compensate=True) if form == "compensate" else {}
+    want = oracle_run(ref, c, plan, **oracle_run_kw)
+    q = TickQueue(dev, records=16)
+    for p in plan:
+        assert q.push(*p), q.error
+    device_run(q, n, [2, 3])
+    assert_same_after_ticks(dev, ref, form)
+    assert [r["substeps"] for r in q.landed(0, n)] == want
+    q.close()

@@ -150,3 +150,27 @@ def test_the_benchmark_configuration_first_steps(gpu):
     assert ws_cases.run(dev, case) == ws_cases.run(ref, case)
     assert_same(dev, ref, "2048")
     dev.close()
+
+
+@pytest.mark.parametrize("nx,ny,edges", [(1, 1, 15), (1, 37, 3), (45, 3, 12), (17, 33, 5),
+                                         (64, 1, 0)])
+def test_odd_and_degenerate_grids(gpu, nx, ny, edges):
+    """Single cells, single rows and columns, odd sizes, every edge combination, everything on."""
+    n = nx * ny
+    rng = np.random.default_rng(nx * 1000 + ny)
+    bed = rng.uniform(0.0, 0.3, n)
+    case = dict(config=dict(nx=nx, ny=ny, cell_m=0.5, open_edges=edges,
+                            carried=[(3.0, 1e-3, 0.0), (0.0, 0.0, 0.0)]),
+                fields=dict(depth=rng.uniform(0.0, 0.4, n), momentum_x=0.02 * rng.standard_normal(n),
+                            momentum_y=0.02 * rng.standard_normal(n), ground=np.zeros(n),
+                            carried=np.concatenate([np.zeros(n), rng.uniform(0, 0.01, n)])),
+                inputs=dict(bed=bed, manning=np.full(n, 0.02), source=rng.uniform(-1e-3, 1e-3, n),
+                            ground_k=np.full(n, 1e-5), ground_s=np.full(n, 0.05),
+                            ground_cap=np.full(n, 0.02),
+                            carried_source=[None, None],
+                            carried_exchange=[None, rng.uniform(-2e-4, 1e-4, n)]),
+                run=[("step", 0.02), ("advance", 0.5)])
+    dev, ref = device_solver(case), oracle_solver(case)
+    assert ws_cases.run(dev, case) == ws_cases.run(ref, case)
+    assert_same(dev, ref, f"{nx}x{ny}")
+    dev.close()
