@@ -100,6 +100,32 @@ __device__ void fold_warp(const Partial* rec, uint32_t groups, float* s) {
   }
 }
 
+// The same by a CTA of 256 threads, a thread a virtual lane: the records of each lane in flight at
+// once rather than a warp's eight lanes one after another (the block tick's first item, on a small
+// tile's critical path). The same sums in the same order.
+__device__ void fold_block(const Partial* rec, uint32_t groups, float* s) {
+  const int t = threadIdx.x;
+  float src = 0.0f, opn = 0.0f, rnd = 0.0f;
+  for (uint32_t gi = t; gi < groups; gi += kGroupCells) {
+    const Partial p = rec[gi];
+    src = __fadd_rn(src, p.source_m3);
+    opn = __fadd_rn(opn, p.open_m3);
+    rnd = __fadd_rn(rnd, p.roundoff_m3);
+  }
+  s[t] = src;
+  s[kGroupCells + t] = opn;
+  s[2 * kGroupCells + t] = rnd;
+  __syncthreads();
+  for (int stride = kGroupCells / 2; stride > 0; stride >>= 1) {
+    if (t < stride) {
+      s[t] = __fadd_rn(s[t], s[t + stride]);
+      s[kGroupCells + t] = __fadd_rn(s[kGroupCells + t], s[kGroupCells + t + stride]);
+      s[2 * kGroupCells + t] = __fadd_rn(s[2 * kGroupCells + t], s[2 * kGroupCells + t + stride]);
+    }
+    __syncthreads();
+  }
+}
+
 // The same with a CTA of 256 threads, the records' sums cleared after they are read and their
 // largest speeds returned (the length pass, slang:412-456).
 __device__ void fold_cta(Partial* rec, uint32_t groups, float* s, uint32_t* s_ab) {
@@ -774,6 +800,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
 // No thread's work waits on a row before it: a tile's faces are as many independent threads as the
 // device holds, where the march's warps walk their rows one after another.
 constexpr int kBlkW = 32, kBlkH = 16, kBlkThreads = 256;
+static_assert(kBlkThreads == int(kGroupCells), "fold_block takes a thread a virtual lane");
 
 struct BlockSmem {
   float4 cell[kBlkH + 2][kBlkW + 2];  // local (r, c) at [r + 1][c + 1]
@@ -816,16 +843,16 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
     const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
-    if (local == 0u && warp == 0) {
-      // dt_main's fold of the last update's records (slang:417-478), into the ledger's next slot.
-      fold_warp(T.rec[rec], T.groups_x * T.groups_y, m.fold);
-      if (lane == 0) {
+    if (local == 0u) {
+      // dt_main's fold of the last update's records (slang:417-478) by the whole CTA, a thread a
+      // virtual lane, into the ledger's next slot.
+      fold_block(T.rec[rec], T.groups_x * T.groups_y, m.fold);
+      if (t == 0) {
         LedgerBits l = ctl->ledger[rec];
         ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
                              T.cfl, T.cell_m, a.max_dt);
         T.ctl->ledger[rec ^ 1u] = l;
       }
-      __syncwarp();
     }
     const int nx = int(T.nx), ny = int(T.ny);
     const size_t n = size_t(T.nx) * T.ny;
