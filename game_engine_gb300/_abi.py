@@ -179,6 +179,7 @@ SIGNATURES = {
     "wl_adjoint_run": (C.c_int, [C.c_void_p, C.c_float, C.c_int, *_err]),
     "wl_adjoint_read": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _u32p, *_err]),
     "wl_adjoint_read_final": (C.c_int, [C.c_void_p, _fp, *_err]),
+    "wl_adjoint_read_state_gradient": (C.c_int, [C.c_void_p, _fp, *_err]),
     "wl_adjoint_launches": (C.c_uint32, [C.c_void_p]),
     "wl_adjoint_device_bytes": (C.c_uint64, [C.c_void_p]),
     # one tick that allocates nothing

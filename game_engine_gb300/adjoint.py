@@ -110,6 +110,14 @@ class Adjoint:
                                                 len(self._buf)))
         return out
 
+    def read_state_gradient(self):
+        """dL/d(starting state): three planes (dL/dh, dL/dhu, dL/dhv) a tile, tile after tile
+        (flat, FP32)."""
+        out = np.zeros(3 * self.cells, dtype=np.float32)
+        self._check(lib().wl_adjoint_read_state_gradient(self._h, out.ctypes.data_as(_fp),
+                                                         self._buf, len(self._buf)))
+        return out
+
     def launches(self) -> int:
         return int(lib().wl_adjoint_launches(self._h))
 

@@ -1072,6 +1072,17 @@ int Adjoint::read_final(float* planes, std::string* err) {
   return WL_OK;
 }
 
+int Adjoint::read_state_gradient(float* planes, std::string* err) {
+  // Reverse tick t writes lam[t & 1], so tick 0's adjoint state is in lam_base_[0], laid out as
+  // the tiles' states are (3 planes a tile, tile after tile).
+  const cudaError_t e = cudaMemcpy(planes, lam_base_[0], lam_bytes_, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_err(err, std::string("water_live: read-back: ") + cudaGetErrorString(e));
+    return WL_ERR_CUDA;
+  }
+  return WL_OK;
+}
+
 }  // namespace wlc
 
 // ---- the C ABI (include/wlcuda.h) ------------------------------------------------------------
@@ -1137,6 +1148,13 @@ int wl_adjoint_read_final(wl_adjoint* a, float* planes, char* err, size_t err_le
   if (planes == nullptr) return put(err, err_len, WL_ERR_ARGUMENT, "water_live: no buffer");
   std::string msg;
   return put(err, err_len, a->impl.read_final(planes, &msg), msg);
+}
+
+int wl_adjoint_read_state_gradient(wl_adjoint* a, float* planes, char* err, size_t err_len) {
+  if (a == nullptr) return put(err, err_len, WL_ERR_INVALID, "water_live: no sweep");
+  if (planes == nullptr) return put(err, err_len, WL_ERR_ARGUMENT, "water_live: no buffer");
+  std::string msg;
+  return put(err, err_len, a->impl.read_state_gradient(planes, &msg), msg);
 }
 
 uint32_t wl_adjoint_launches(const wl_adjoint* a) { return a ? a->impl.launches() : 0u; }

@@ -97,6 +97,8 @@ class Adjoint {
   int read(double* loss, double* g_bed, double* g_src, uint32_t* limited, std::string* err);
   // The state of tick T (3 planes a tile, tile after tile).
   int read_final(float* planes, std::string* err);
+  // dL/d(state of tick 0), the reverse sweep's last adjoint state (3 planes a tile, tile after tile).
+  int read_state_gradient(float* planes, std::string* err);
   uint32_t launches() const;
   uint64_t device_bytes() const { return bytes_; }
   int rows() const { return rows_; }

@@ -293,6 +293,9 @@ int wl_adjoint_read(wl_adjoint* adjoint, double* loss, double* g_bed, double* g_
                     uint32_t* limited, char* err, size_t err_len);
 /* The state of tick T: three planes (h, hu, hv) a tile, tile after tile. */
 int wl_adjoint_read_final(wl_adjoint* adjoint, float* planes, char* err, size_t err_len);
+/* dL/d(starting state): three planes (dL/dh, dL/dhu, dL/dhv) a tile, tile after tile, FP32 (the
+ * sweep's adjoint state after its last reverse tick). */
+int wl_adjoint_read_state_gradient(wl_adjoint* adjoint, float* planes, char* err, size_t err_len);
 /* Kernel launches in one sweep, and the sweep's device bytes. */
 uint32_t wl_adjoint_launches(const wl_adjoint* adjoint);
 uint64_t wl_adjoint_device_bytes(const wl_adjoint* adjoint);

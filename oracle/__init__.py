@@ -102,7 +102,7 @@ def lib():
                                                      _dp, _dp]
         L.oracle_adjoint.restype = C.c_uint32
         L.oracle_adjoint.argtypes = grid_args + [C.c_int, C.c_double, C.c_uint32, _dp, _dp, _dp,
-                                                 _u32p, _dp, C.c_uint32, _dp, _dp, _dp]
+                                                 _u32p, _dp, C.c_uint32, _dp, _dp, _dp, _dp]
         L.oracle_adjoint_mixed.restype = C.c_uint32
         L.oracle_adjoint_mixed.argtypes = grid_args + [C.c_double, C.c_uint32, _dp, _dp, _dp,
                                                        _u32p, _dp, C.c_uint32, _dp, _dp, _dp]
@@ -383,18 +383,23 @@ def adj_forward(grid: Grid, dt, ticks, bed, source, state0, precision64=False):
     return out.reshape(3, -1), int(lim)
 
 
-def adjoint(grid: Grid, dt, ticks, bed, source, state0, probes, targets, precision64=True):
+def adjoint(grid: Grid, dt, ticks, bed, source, state0, probes, targets, precision64=True,
+            state_gradient=False):
     """The loss sum_p (h_T(p) - target_p)^2 and its gradients with respect to the bed and the
-    source by the reverse sweep. Returns (loss, g_bed, g_source, shortened ticks)."""
+    source by the reverse sweep. Returns (loss, g_bed, g_source, shortened ticks), and with
+    state_gradient the gradient with respect to the starting state (3 planes) after them."""
     bed, source, state0, targets = _keep(bed, source, state0, targets)
     probes = _u32(probes)
     g_bed = np.zeros(grid.cells)
     g_src = np.zeros(grid.cells)
+    g_u0 = np.zeros(3 * grid.cells) if state_gradient else None
     loss = C.c_double(0.0)
     lim = lib().oracle_adjoint(*_grid_args(grid), int(precision64), float(dt), int(ticks),
                                _d(bed), _d(source), _d(state0),
                                probes.ctypes.data_as(C.POINTER(C.c_uint32)), _d(targets),
-                               probes.size, C.byref(loss), _d(g_bed), _d(g_src))
+                               probes.size, C.byref(loss), _d(g_bed), _d(g_src), _d(g_u0))
+    if state_gradient:
+        return loss.value, g_bed, g_src, int(lim), g_u0
     return loss.value, g_bed, g_src, int(lim)
 
 

@@ -288,7 +288,7 @@ void reverse_tick(const Config& c, T dt, const T* bed, const T* src, const T* in
 template <class T>
 u32 adjoint(const Config& c, double dt_d, u32 ticks, const double* bed_d, const double* src_d,
              const double* state0, const u32* probes, const double* targets, u32 n_probes,
-             double* loss, double* g_bed, double* g_src) {
+             double* loss, double* g_bed, double* g_src, double* g_state0 = nullptr) {
   const size_t n = size_t(c.nx) * c.ny;
   const T dt = T(dt_d);
   std::vector<T> bed(n), src;
@@ -324,6 +324,9 @@ u32 adjoint(const Config& c, double dt_d, u32 ticks, const double* bed_d, const 
                     g_src ? g_src : dummy.data());
     lam.swap(lam2);
   }
+  // The adjoint state of tick 0: the gradient with respect to the starting state (h, hu, hv).
+  if (g_state0 != nullptr)
+    for (size_t i = 0; i < 3 * n; ++i) g_state0[i] = double(lam[i]);
   return n_limited;
 }
 

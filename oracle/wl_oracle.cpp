@@ -258,13 +258,13 @@ uint32_t oracle_adjoint(uint32_t nx, uint32_t ny, double cell_m, double gravity,
                         double dry, uint32_t open_edges, int precision64, double dt, uint32_t ticks,
                         const double* bed, const double* src, const double* state0,
                         const uint32_t* probes, const double* targets, uint32_t n_probes,
-                        double* loss, double* g_bed, double* g_src) {
+                        double* loss, double* g_bed, double* g_src, double* g_state0) {
   const Config c = make_config(nx, ny, cell_m, gravity, cfl, dry, open_edges);
   return precision64
              ? adjoint<double>(c, dt, ticks, bed, src, state0, probes, targets, n_probes, loss,
-                               g_bed, g_src)
+                               g_bed, g_src, g_state0)
              : adjoint<float>(c, dt, ticks, bed, src, state0, probes, targets, n_probes, loss,
-                              g_bed, g_src);
+                              g_bed, g_src, g_state0);
 }
 
 // The FP32 forward with the FP64 reverse sweep over it.

@@ -156,3 +156,16 @@ def test_a_full_solver_never_created_refuses_every_call(wl_lib):
     cfg.nx, cfg.carried = 4, 5
     assert wl_lib.ws_create(C.byref(cfg), C.byref(out), err, 128) == 8 and not out.value
     assert C.sizeof(_abi.WsConfig) == 160 and C.sizeof(_abi.WsLedger) == 224
+
+
+def test_an_adjoint_never_created_refuses_every_read(wl_lib):
+    # The sweep's read-backs with no sweep: WL_ERR_INVALID (1); 0 for the count calls.
+    err = C.create_string_buffer(128)
+    buf = (C.c_float * 3)()
+    assert wl_lib.wl_adjoint_read(None, None, None, None, None, err, 128) == 1
+    assert wl_lib.wl_adjoint_read_final(None, buf, err, 128) == 1
+    assert wl_lib.wl_adjoint_read_state_gradient(None, buf, err, 128) == 1
+    assert b"no sweep" in err.value
+    assert wl_lib.wl_adjoint_launches(None) == 0
+    assert wl_lib.wl_adjoint_device_bytes(None) == 0
+    wl_lib.wl_adjoint_destroy(None)

@@ -88,6 +88,28 @@ def test_gradients_are_the_oracle_sweep(gpu, edges, seed, sinks):
     a.close()
 
 
+@pytest.mark.parametrize("edges,seed,sinks", [(0, 7, False), (6, 9, True)])
+def test_the_starting_state_gradient_is_the_oracle_sweep(gpu, edges, seed, sinks):
+    """dL/d(h0, hu0, hv0) read back after the sweep: the oracle's FP32 sweep within 1e-5, its
+    FP64 sweep (pinned to the FP64 replay's central differences on the CPU) within 1e-4."""
+    c = basin(24, 20, seed, edges=edges, sinks=sinks)
+    ticks = 120
+    probes, targets = probes_and_targets(c, ticks, DT, 12, seed=seed)
+    dev = device_step(c)
+    a = Adjoint(dev, ticks, 16, probes, targets)
+    a.run(DT)
+    lam = a.read_state_gradient()
+    args = (grid(c), DT, ticks, c["bed"], c["source"], c["state0"], probes, targets)
+    *_, g32 = oracle.adjoint(*args, precision64=False, state_gradient=True)
+    *_, g64 = oracle.adjoint(*args, precision64=True, state_gradient=True)
+    assert rel_err(lam, g32) < 1e-5
+    assert rel_err(lam, g64) < TOL
+    # a second sweep from the same state gives the same bytes
+    a.run(DT, graph=True)
+    assert np.array_equal(bits(a.read_state_gradient()), bits(lam))
+    a.close()
+
+
 def test_checkpoint_interval_graph_and_replay_change_no_byte(gpu):
     c = basin(50, 37, 4, edges=5, sinks=True)
     ticks = 45
@@ -116,7 +138,7 @@ def test_a_batch_sweep_is_each_tile_swept_alone(gpu):
         dev = device_step(c)
         a = Adjoint(dev, ticks, every, p, t)
         a.run(DT)
-        alone.append(a.read() + (a.read_final(),))
+        alone.append(a.read() + (a.read_final(), a.read_state_gradient()))
         a.close()
         tiles.append(c)
         probes.append(p)
@@ -129,14 +151,16 @@ def test_a_batch_sweep_is_each_tile_swept_alone(gpu):
     a.run(DT)
     loss, g_bed, g_src, limited = a.read()
     fin = a.read_final()
+    lam = a.read_state_gradient()
     first, first3 = 0, 0
     for k, c in enumerate(tiles):
         n = c["nx"] * c["ny"]
-        l1, gb1, gs1, lim1, fin1 = alone[k]
+        l1, gb1, gs1, lim1, fin1, lam1 = alone[k]
         assert loss[k] == l1[0] and limited[k] == lim1[0]
         assert np.array_equal(g_bed[first:first + n], gb1)
         assert np.array_equal(g_src[first:first + n], gs1)
         assert np.array_equal(bits(fin[first3:first3 + 3 * n]), bits(fin1))
+        assert np.array_equal(bits(lam[first3:first3 + 3 * n]), bits(lam1))
         first += n
         first3 += 3 * n
     a.close()
