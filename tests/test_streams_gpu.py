@@ -67,6 +67,25 @@ def test_plain_2048_first_ticks_bit_exact(gpu):
     assert_same(dev, ref, "plain_2048, 3 ticks")
 
 
+@pytest.mark.parametrize("fixed", [False, True])
+def test_a_tile_of_more_items_than_warps(gpu, fixed):
+    """1024 x 2080 (32 x 130 items of 32 x 16 rows, more than the device holds warps, so warps take
+    items in rounds, the last round part-filled): open west and south edges, rain with sinks, 40
+    ticks, every state word, record and ledger byte against the oracle."""
+    nx, ny = 1024, 2080
+    bed = workloads.fbm(nx, ny, 8.0, 77)
+    rng = np.random.default_rng(77)
+    h = rng.uniform(0.0, 0.6, nx * ny)
+    source = np.where(rng.random(nx * ny) < 0.05, -2e-3, 1e-3)
+    c = dict(nx=nx, ny=ny, cell_m=1.0, bed=bed, h=h, source=source, open_edges=5)
+    dev, ref = make_pair(c, fixed=fixed, rows=16)
+    for k in (1, 39):
+        assert dev.run_steps(k, 0.01), dev.error
+        ref.run_steps(k, 0.01)
+        assert_same(dev, ref, f"1024x2080 after +{k}")
+    assert dev.read_ledger()["open_edge_out_m3"] != 0.0
+
+
 def test_plain_2048_full_run_properties(gpu):
     # 500 ticks of rain: the same bytes twice, and the ledger's balance of the water.
     from pairs import config
