@@ -94,7 +94,8 @@ std::vector<uint32_t> item_order(const std::vector<wlc::TileSpec>& specs, uint32
 // What a captured graph depends on: the block shape, the order, the launch's grid and variant.
 uint64_t launch_key(const wl_batch* b) {
   return (uint64_t(b->set.shape()) << 48) ^ (uint64_t(b->tuning.order) << 40) ^
-         (uint64_t(b->set.grid()) << 8) ^ (b->set.any_manning() ? 1u : 0u);
+         (uint64_t(b->set.grid()) << 8) ^ (b->set.any_manning() ? 1u : 0u) ^
+         (b->set.plain() ? 2u : 0u);
 }
 
 void drop_graphs(wl_batch* b) {

@@ -21,6 +21,9 @@ constexpr uint32_t kFlagManning = 16u;
 constexpr uint32_t kFlagSource = 32u;
 constexpr uint32_t kFlagCompensate = 64u;
 constexpr uint32_t kFlagStoredFaces = 128u;
+// The flags the march's plain variant compiles out (it runs where no tile holds one).
+constexpr uint32_t kFlagsNotPlain = kFlagWestOpen | kFlagEastOpen | kFlagSouthOpen |
+                                    kFlagNorthOpen | kFlagManning | kFlagCompensate;
 constexpr uint32_t kGroupSide = 16u;
 constexpr uint32_t kGroupCells = 256u;
 constexpr uint32_t kStatePlanes = 4u;

@@ -445,7 +445,7 @@ __device__ __forceinline__ void split_partials(float* ring, int ring_row0, int r
 // are rows ring_row0 .. ring_row0 + H - 1 of a 16-row item that the CTA's warps share; their
 // volumes go to the CTA's ring and the records are the CTA's (split_partials, then group_records
 // after the CTA's barrier).
-template <bool FIXED, bool MANNING, int H, bool SPLIT>
+template <bool FIXED, bool MANNING, int H, bool SPLIT, bool PLAIN = false>
 __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, float* ring,
                       int ring_row0, uint32_t* s_ab, uint32_t* s_need, uint32_t& ia,
                       uint32_t& ib) {
@@ -506,10 +506,11 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
     return;
   }
 
-  const float sw = (flags & kFlagWestOpen) ? 1.0f : -1.0f;
-  const float se = (flags & kFlagEastOpen) ? 1.0f : -1.0f;
-  const float ss = (flags & kFlagSouthOpen) ? 1.0f : -1.0f;
-  const float sn = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
+  // PLAIN: every edge closed, no compensated source, no Manning (none of kFlagsNotPlain is set).
+  const float sw = (!PLAIN && (flags & kFlagWestOpen)) ? 1.0f : -1.0f;
+  const float se = (!PLAIN && (flags & kFlagEastOpen)) ? 1.0f : -1.0f;
+  const float ss = (!PLAIN && (flags & kFlagSouthOpen)) ? 1.0f : -1.0f;
+  const float sn = (!PLAIN && (flags & kFlagNorthOpen)) ? 1.0f : -1.0f;
 
   // The band's side columns, a row a lane: the west neighbour of lane 0 as {h, z, u, v} (a ghost
   // at the west edge, slang:597-600), and the east face of the last live lane (against its east
@@ -571,9 +572,9 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   const float lam = O::div(dt, cell_m);
   const float edge_volume = __fmul_rn(dt, cell_m);
   const bool src_on = it.apply_source != 0u;
-  const bool comp = (flags & kFlagCompensate) != 0u;
-  const bool manning = MANNING && (flags & kFlagManning) != 0u;
-  const bool any_open_band = (flags & 15u) != 0u;
+  const bool comp = !PLAIN && (flags & kFlagCompensate) != 0u;
+  const bool manning = !PLAIN && MANNING && (flags & kFlagManning) != 0u;
+  const bool any_open_band = !PLAIN && (flags & 15u) != 0u;
   const float scale = it.scale;
   bool opn_seen = false, rnd_seen = false;
   const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
@@ -653,9 +654,11 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   if (SPLIT) split_partials(ring, ring_row0, rows, ga, gb, opn_seen, rnd_seen, s_ab, s_need);
 }
 
-// The persistent tick: every work item of every tile, one tick.
-template <bool FIXED, bool MANNING, int H>
-__global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
+// The persistent tick: every work item of every tile, one tick. PLAIN (no tile holds a flag of
+// kFlagsNotPlain) compiles the open edges, the compensated source and Manning out of the march,
+// which then fits 80 registers: six CTAs an SM instead of five.
+template <bool FIXED, bool MANNING, int H, bool PLAIN>
+__global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickArgs a) {
   if (a.go != nullptr && *a.go == 0u) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const WarpMem<H> wm = warp_mem<H>(warp);
@@ -696,7 +699,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_kernel(TickArgs a) {
       __syncwarp();
     }
     uint32_t ia = 0u, ib = 0u;
-    march<FIXED, MANNING, H, false>(T, it, wm, wm.ring, 0, nullptr, nullptr, ia, ib);
+    march<FIXED, MANNING, H, false, PLAIN>(T, it, wm, wm.ring, 0, nullptr, nullptr, ia, ib);
     __syncwarp();
     // `rec` read again rather than held through the march (a register fewer): only the tile's
     // last item flips it, after this item's count.
@@ -1303,22 +1306,31 @@ cudaError_t split_launch(bool fixed, bool manning, const TickArgs& a, int grid, 
   return cudaGetLastError();
 }
 
+// The march's variants: Manning's, the plain one (where `plain` and no Manning), the general one.
 template <int H>
-const void* tick_fn(bool fixed, bool manning) {
-  if (fixed)
-    return manning ? (const void*)tick_kernel<true, true, H> : (const void*)tick_kernel<true, false, H>;
-  return manning ? (const void*)tick_kernel<false, true, H> : (const void*)tick_kernel<false, false, H>;
+const void* tick_fn(bool fixed, bool manning, bool plain) {
+  if (fixed) {
+    if (manning) return (const void*)tick_kernel<true, true, H, false>;
+    return plain ? (const void*)tick_kernel<true, false, H, true>
+                 : (const void*)tick_kernel<true, false, H, false>;
+  }
+  if (manning) return (const void*)tick_kernel<false, true, H, false>;
+  return plain ? (const void*)tick_kernel<false, false, H, true>
+               : (const void*)tick_kernel<false, false, H, false>;
 }
 
 template <int H>
-cudaError_t tick_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
+cudaError_t tick_launch(bool fixed, bool manning, bool plain, const TickArgs& a, int grid,
+                        cudaStream_t s) {
   const size_t smem = kWarpsPerCta * WarpMem<H>::kBytes;
   if (fixed) {
-    if (manning) tick_kernel<true, true, H><<<grid, kCtaThreads, smem, s>>>(a);
-    else tick_kernel<true, false, H><<<grid, kCtaThreads, smem, s>>>(a);
+    if (manning) tick_kernel<true, true, H, false><<<grid, kCtaThreads, smem, s>>>(a);
+    else if (plain) tick_kernel<true, false, H, true><<<grid, kCtaThreads, smem, s>>>(a);
+    else tick_kernel<true, false, H, false><<<grid, kCtaThreads, smem, s>>>(a);
   } else {
-    if (manning) tick_kernel<false, true, H><<<grid, kCtaThreads, smem, s>>>(a);
-    else tick_kernel<false, false, H><<<grid, kCtaThreads, smem, s>>>(a);
+    if (manning) tick_kernel<false, true, H, false><<<grid, kCtaThreads, smem, s>>>(a);
+    else if (plain) tick_kernel<false, false, H, true><<<grid, kCtaThreads, smem, s>>>(a);
+    else tick_kernel<false, false, H, false><<<grid, kCtaThreads, smem, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -1368,12 +1380,12 @@ void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
   by = 0;
 }
 
-int tick_occupancy(BlockShape shape, bool fixed, bool manning) {
+int tick_occupancy(BlockShape shape, bool fixed, bool manning, bool plain) {
   const void* fn = nullptr;
   switch (shape) {
-    case BlockShape::k32x16: fn = tick_fn<16>(fixed, manning); break;
-    case BlockShape::k32x32: fn = tick_fn<32>(fixed, manning); break;
-    case BlockShape::k32x64: fn = tick_fn<64>(fixed, manning); break;
+    case BlockShape::k32x16: fn = tick_fn<16>(fixed, manning, plain); break;
+    case BlockShape::k32x32: fn = tick_fn<32>(fixed, manning, plain); break;
+    case BlockShape::k32x64: fn = tick_fn<64>(fixed, manning, plain); break;
     case BlockShape::k32x16s: fn = split_fn(fixed, manning); break;
     case BlockShape::k32x16b: fn = block_fn(fixed, manning); break;
   }
@@ -1387,12 +1399,12 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning) {
   return blocks;
 }
 
-cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickArgs& a, int grid,
-                        cudaStream_t s) {
+cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain, const TickArgs& a,
+                        int grid, cudaStream_t s) {
   switch (shape) {
-    case BlockShape::k32x16: return tick_launch<16>(fixed, manning, a, grid, s);
-    case BlockShape::k32x32: return tick_launch<32>(fixed, manning, a, grid, s);
-    case BlockShape::k32x64: return tick_launch<64>(fixed, manning, a, grid, s);
+    case BlockShape::k32x16: return tick_launch<16>(fixed, manning, plain, a, grid, s);
+    case BlockShape::k32x32: return tick_launch<32>(fixed, manning, plain, a, grid, s);
+    case BlockShape::k32x64: return tick_launch<64>(fixed, manning, plain, a, grid, s);
     case BlockShape::k32x16s: return split_launch(fixed, manning, a, grid, s);
     case BlockShape::k32x16b: return block_launch(fixed, manning, a, grid, s);
   }

@@ -33,11 +33,12 @@ size_t tick_smem_bytes(BlockShape shape);
 int tick_threads(BlockShape shape);
 void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by);
 // Sets the kernels' shared-memory opt-in on the current device and returns the resident CTAs per
-// SM (0 on an error).
-int tick_occupancy(BlockShape shape, bool fixed, bool manning);
+// SM (0 on an error). `manning`: some tile holds Manning's n; `plain`: no tile holds a flag of
+// kFlagsNotPlain (the march's plain variant; the split and block shapes have none).
+int tick_occupancy(BlockShape shape, bool fixed, bool manning, bool plain);
 
-cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, const TickArgs& a, int grid,
-                        cudaStream_t s);
+cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain, const TickArgs& a,
+                        int grid, cudaStream_t s);
 // The records of the states just written (one CTA a work item, the same items as the tick's).
 cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaStream_t s);
 cudaError_t launch_length_pass(bool fixed, const TileDesc* tiles, uint32_t tile, float max_dt,

@@ -143,7 +143,8 @@ extern "C" int wl_tick_noalloc(const wl_config* config, int fixed_ops, const flo
   d.items = d.blocks_x * d.blocks_y;
 
   const bool fixed = fixed_ops != 0, with_manning = manning != nullptr;
-  const int occ = tick_occupancy(shape, fixed, with_manning);
+  const bool plain = (d.flags & kFlagsNotPlain) == 0u;
+  const int occ = tick_occupancy(shape, fixed, with_manning, plain);
   if (occ <= 0) return put(err, err_len, WL_ERR_CUDA, "water_live: the tick cannot be resident");
   const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   static_init_kernel<<<1, 32, 0, st>>>(s, d);
@@ -152,7 +153,7 @@ extern "C" int wl_tick_noalloc(const wl_config* config, int fixed_ops, const flo
   if (e == cudaSuccess) e = launch_prime(shape, fixed, a, st);  // the input's records
   a.max_dt = max_dt;
   const int grid = int(std::min<uint64_t>(d.items, uint64_t(sms) * occ));
-  if (e == cudaSuccess) e = launch_tick(shape, fixed, with_manning, a, grid, st);
+  if (e == cudaSuccess) e = launch_tick(shape, fixed, with_manning, plain, a, grid, st);
   if (e != cudaSuccess)
     return put(err, err_len, WL_ERR_CUDA, std::string("water_live: ") + cudaGetErrorString(e));
   return WL_OK;

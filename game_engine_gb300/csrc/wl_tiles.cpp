@@ -98,6 +98,12 @@ bool TileSet::any_manning() const {
   return false;
 }
 
+bool TileSet::plain() const {
+  for (const TileDesc& d : host_)
+    if (d.flags & kFlagsNotPlain) return false;
+  return true;
+}
+
 bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_ops,
                      BlockShape shape, const std::vector<uint32_t>& order, std::string* err) {
   destroy();
@@ -224,8 +230,8 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   }
   for (BlockShape s : {BlockShape::k32x16, BlockShape::k32x32, BlockShape::k32x64,
                        BlockShape::k32x16s, BlockShape::k32x16b})
-    for (bool m : {false, true})
-      if (tick_occupancy(s, fixed_, m) <= 0) {
+    for (int v = 0; v < 3; ++v)  // Manning's, the plain and the general variant
+      if (tick_occupancy(s, fixed_, v == 0, v == 1) <= 0) {
         if (err) *err = "water_live: the tick kernel cannot be resident on this device";
         destroy();
         return false;
@@ -275,7 +281,7 @@ bool TileSet::layout_items(BlockShape shape, const std::vector<uint32_t>& order,
   if (!check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), err,
              "cudaDeviceGetAttribute"))
     return false;
-  const int occ = tick_occupancy(shape, fixed_, any_manning());
+  const int occ = tick_occupancy(shape, fixed_, any_manning(), plain());
   grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
   // The items' tile indices: a separate small allocation, replaced on a reshape.
   static_assert(sizeof(uint32_t) == 4, "");
@@ -324,9 +330,9 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   a.n_items = n_items_;
   a.max_dt = max_dt;
   a.go = go;
-  const bool manning = any_manning();
+  const bool manning = any_manning(), plain_set = plain();
   for (uint32_t i = 0; i < count; ++i) {
-    const cudaError_t e = launch_tick(shape_, fixed_, manning, a, grid_, s);
+    const cudaError_t e = launch_tick(shape_, fixed_, manning, plain_set, a, grid_, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -342,9 +348,10 @@ cudaError_t TileSet::enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
   const bool manning = (host_[tile].flags & kFlagManning) != 0u;
-  const int occ = std::max(1, tick_occupancy(shape_, fixed_, manning));
+  const bool plain_tile = (host_[tile].flags & kFlagsNotPlain) == 0u;
+  const int occ = std::max(1, tick_occupancy(shape_, fixed_, manning, plain_tile));
   const int grid = std::max(1, std::min<int>(int(a.n_items), sms * occ));
-  return launch_tick(shape_, fixed_, manning, a, grid, s);
+  return launch_tick(shape_, fixed_, manning, plain_tile, a, grid, s);
 }
 
 cudaError_t TileSet::enqueue_prime(cudaStream_t s) {
@@ -465,7 +472,7 @@ bool TileSet::set_flags(uint32_t tile, uint32_t flags, uint32_t source_every, bo
   // The launch grid follows the variant the flags select.
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
-  const int occ = tick_occupancy(shape_, fixed_, any_manning());
+  const int occ = tick_occupancy(shape_, fixed_, any_manning(), plain());
   grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
   return true;
 }
@@ -588,7 +595,7 @@ bool TileSet::set_flags_all(uint32_t flags_set, uint32_t flags_clear, uint32_t s
     return false;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
-  const int occ = tick_occupancy(shape_, fixed_, any_manning());
+  const int occ = tick_occupancy(shape_, fixed_, any_manning(), plain());
   grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
   return wait(err);
 }

@@ -97,6 +97,8 @@ class TileSet {
   TileDesc* device_descs() const { return d_desc_; }
   float* device_state(uint32_t tile, uint32_t copy) const { return host_[tile].state[copy]; }
   bool any_manning() const;
+  // No tile holds a flag of kFlagsNotPlain: the tick launches the march's plain variant.
+  bool plain() const;
 
  private:
   bool check(cudaError_t e, std::string* err, const char* what);

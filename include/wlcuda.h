@@ -146,7 +146,10 @@ int wl_set_source(wl_step* step, const double* source_m_per_s, size_t n, uint32_
 /* DeviceStep::record (water_live.cpp:488-568) onto a stream: `count` ticks of
  * min(stable step, max_dt, time left), one kernel launch each; nothing waits. Every per-tick
  * quantity (which copy holds the state, the step's length, the ledger, the source clock) lives on
- * the device, so a captured graph of these launches may be replayed any number of times. */
+ * the device, so a captured graph of these launches may be replayed any number of times. The
+ * kernel each launch runs is chosen when it is enqueued, from the step's flags (Manning on, the
+ * compensated source, open edges): a graph captured before wl_set_manning or wl_set_source changes
+ * those must be captured again. */
 int wl_enqueue_steps(wl_step* step, wl_stream stream, uint32_t count, float max_dt);
 /* DeviceStep::run_steps (water_live.cpp:570-574): enqueued on the step's own stream and waited for. */
 int wl_run_steps(wl_step* step, uint32_t count, float max_dt, char* err, size_t err_len);
