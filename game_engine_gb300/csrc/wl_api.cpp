@@ -95,6 +95,8 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
   *out = nullptr;
   if (config->nx == 0 || config->ny == 0)  // water_live.cpp:108
     return fail(err, err_len, WL_ERR_SIZE, "water_live: an empty grid");
+  if (uint64_t(config->nx) * config->ny > wlc::kMaxTileCells)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a grid of more than 2^30 cells");
   auto* s = new (std::nothrow) wl_step;
   if (s == nullptr) return fail(err, err_len, WL_ERR_ALLOC, "water_live: out of host memory");
   s->config = *config;

@@ -187,6 +187,10 @@ int wl_batch_create(const wl_config* common, const wl_options* options, const wl
       delete b;
       return fail(err, err_len, WL_ERR_SIZE, "water_live: an empty grid");
     }
+    if (uint64_t(tiles[i].nx) * tiles[i].ny > wlc::kMaxTileCells) {
+      delete b;
+      return fail(err, err_len, WL_ERR_SIZE, "water_live: a grid of more than 2^30 cells");
+    }
     wlc::TileSpec& s = b->specs[i];
     s.nx = tiles[i].nx;
     s.ny = tiles[i].ny;

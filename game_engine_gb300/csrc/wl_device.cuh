@@ -27,6 +27,8 @@ constexpr uint32_t kFlagsNotPlain = kFlagWestOpen | kFlagEastOpen | kFlagSouthOp
 constexpr uint32_t kGroupSide = 16u;
 constexpr uint32_t kGroupCells = 256u;
 constexpr uint32_t kStatePlanes = 4u;
+// The largest tile: the kernels index a tile's cells, and its planes' cells, in 32 bits.
+constexpr uint64_t kMaxTileCells = uint64_t(1) << 30;
 constexpr int kThreads = 256;  // one CTA: 8 warps; also the length pass's 256 lanes
 
 // water_live::WaterPartial (water_live.h:114-121).

@@ -471,6 +471,9 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   float* qhu = out + n;
   float* qhv = out + 2 * n;
   const float* bed = T.bed;
+  // The row loop addresses the three state planes from one base and 32-bit offsets (a tile holds
+  // at most 2^30 cells): fewer live 64-bit pointers, fewer spills in the plain variant.
+  const uint32_t n32 = uint32_t(n);
   // The planes the rows read, in registers: the march's stores could alias the descriptor.
   const float* source = T.source;
   const float* manning_n = T.manning;
@@ -594,9 +597,9 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
     // The row two ahead, in flight while this row computes.
     if (gy + 2 < ny) {
       const int k = i + 2 * nx;
-      nh = ph[k];
-      nhu = phu[k];
-      nhv = phv[k];
+      nh = in[k];
+      nhu = in[n32 + uint32_t(k)];
+      nhv = in[2u * n32 + uint32_t(k)];
       nz = bed[k];
       if (src_on) nsrc = source[k];
     }
@@ -614,9 +617,9 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
       update_cell<FIXED>(uc, c, hu, hv, src, comp ? in[3 * n + i] : 0.0f,
                          manning ? manning_n[i] : 0.0f, fw, fe, fs, fn, gx, gy, h, mu, mv,
                          residual, csrc, copn, crnd);
-      qh[i] = h;
-      qhu[i] = mu;
-      qhv[i] = mv;
+      out[i] = h;
+      out[n32 + uint32_t(i)] = mu;
+      out[2u * n32 + uint32_t(i)] = mv;
       if (comp) out[3 * n + i] = residual;
       cell_speeds<FIXED>(g, dry, h, mu, mv, ax, ay);
     }

@@ -110,7 +110,9 @@ typedef struct wl_step wl_step;
 
 /* ---- the plain step: water_live::DeviceStep (water_live.cpp:105-639) ---------------------- */
 
-/* DeviceStep::create (water_live.cpp:105-210): the state dry over a bed of zero, the ledger empty. */
+/* DeviceStep::create (water_live.cpp:105-210): the state dry over a bed of zero, the ledger empty.
+ * An empty grid, or one of more than 2^30 cells (a tile's cells are indexed in 32 bits), is
+ * refused with WL_ERR_SIZE; wl_batch_create refuses such a tile the same way. */
 int wl_create(const wl_config* config, const wl_options* options, wl_step** out, char* err,
               size_t err_len);
 /* DeviceStep::destroy (water_live.cpp:212-229). Null is a no-op. */

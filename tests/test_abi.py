@@ -92,6 +92,10 @@ def test_an_empty_grid_is_refused(wl_lib):
     assert wl_lib.wl_create(C.byref(cfg), None, C.byref(out), err, 128) == 2
     assert b"empty grid" in err.value
     assert not out.value
+    # A tile's cells are indexed in 32 bits: more than 2^30 cells is refused the same way.
+    big = _abi.Config(32768, 32769, 1.0, 9.81, 0.45, 1e-9, 0, 0, 0, 0, 0)
+    assert wl_lib.wl_create(C.byref(big), None, C.byref(out), err, 128) == 2
+    assert b"2^30" in err.value and not out.value
 
 
 def test_the_numerics_policy_of_every_build():
