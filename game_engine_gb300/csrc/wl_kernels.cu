@@ -104,17 +104,19 @@ __device__ void fold_warp(const Partial* rec, uint32_t groups, float* s) {
 // once rather than a warp's eight lanes one after another (the block tick's first item, on a small
 // tile's critical path). The same sums in the same order.
 __device__ void fold_block(const Partial* rec, uint32_t groups, float* s) {
-  const int t = threadIdx.x;
-  float src = 0.0f, opn = 0.0f, rnd = 0.0f;
-  for (uint32_t gi = t; gi < groups; gi += kGroupCells) {
-    const Partial p = rec[gi];
-    src = __fadd_rn(src, p.source_m3);
-    opn = __fadd_rn(opn, p.open_m3);
-    rnd = __fadd_rn(rnd, p.roundoff_m3);
+  const int t = threadIdx.x;  // threads past the 256 virtual lanes take only the barriers
+  if (t < int(kGroupCells)) {
+    float src = 0.0f, opn = 0.0f, rnd = 0.0f;
+    for (uint32_t gi = t; gi < groups; gi += kGroupCells) {
+      const Partial p = rec[gi];
+      src = __fadd_rn(src, p.source_m3);
+      opn = __fadd_rn(opn, p.open_m3);
+      rnd = __fadd_rn(rnd, p.roundoff_m3);
+    }
+    s[t] = src;
+    s[kGroupCells + t] = opn;
+    s[2 * kGroupCells + t] = rnd;
   }
-  s[t] = src;
-  s[kGroupCells + t] = opn;
-  s[2 * kGroupCells + t] = rnd;
   __syncthreads();
   for (int stride = kGroupCells / 2; stride > 0; stride >>= 1) {
     if (t < stride) {
@@ -797,16 +799,18 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
 
 // ---- the block tick -------------------------------------------------------------------------
 //
-// A CTA of 256 threads steps one 32 x 16 block (the 32 x 16 items, two 16 x 16 groups) at a time
-// in three phases through shared memory:
+// A CTA of THREADS threads steps one 32 x 16 block (the 32 x 16 items, two 16 x 16 groups) at a
+// time in three phases through shared memory:
 //   1. the block's cells and a one-cell halo as {h, z, u, v} (ghosts at the tile's edges);
 //   2. every face of the block, one a thread (a face on the block's boundary is computed by both
 //      blocks that share it);
 //   3. every cell's update from its four faces, then the block's two records.
 // No thread's work waits on a row before it: a tile's faces are as many independent threads as the
 // device holds, where the march's warps walk their rows one after another.
-constexpr int kBlkW = 32, kBlkH = 16, kBlkThreads = 256;
-static_assert(kBlkThreads == int(kGroupCells), "fold_block takes a thread a virtual lane");
+// THREADS 256 (two cells and about four faces a thread) packs four CTAs an SM; 512 (one cell and
+// about two faces a thread) halves each thread's share of a block, which is what a launch of no
+// more blocks than SMs (a small tile) waits for: its tick is one CTA's chain of phases.
+constexpr int kBlkW = 32, kBlkH = 16, kBlkThreads = 256, kBlkWideThreads = 512;
 
 struct BlockSmem {
   float4 cell[kBlkH + 2][kBlkW + 2];  // local (r, c) at [r + 1][c + 1]
@@ -817,8 +821,12 @@ struct BlockSmem {
   uint32_t item, need, ab[4];
 };
 
-template <bool FIXED, bool MANNING>
-__global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) {
+template <bool FIXED, bool MANNING, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(TickArgs a) {
+  static_assert(THREADS >= int(kGroupCells) && THREADS % 32 == 0,
+                "fold_block takes a thread a virtual lane");
+  static_assert(THREADS >= 2 * kBlkW + 2 * kBlkH, "a thread a halo cell");
+  constexpr int kBlkWarps = THREADS / 32;
   if (a.go != nullptr && *a.go == 0u) return;
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
@@ -868,14 +876,15 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
     const float* bed = T.bed;
     const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
     const uint32_t flags = T.flags;
-    // The two cells this thread updates: (t >> 5, t & 31) and (8 + (t >> 5), t & 31).
+    // The cells this thread updates: rows warp + kBlkWarps k of column t & 31.
+    constexpr int K = (kBlkH + kBlkWarps - 1) / kBlkWarps;
     const int cc = lane;
-    float rh[2], rhu[2], rhv[2];
-    bool live[2];
-    int gi[2];
+    float rh[K], rhu[K], rhv[K];
+    bool live[K];
+    int gi[K];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const int r = warp + 8 * k;
+    for (int k = 0; k < K; ++k) {
+      const int r = warp + kBlkWarps * k;
       live[k] = r < rows && cc < cols;
       gi[k] = (Y0 + r) * nx + X0 + cc;
       rh[k] = rhu[k] = rhv[k] = 0.0f;
@@ -890,7 +899,7 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
     if (!(dt > 0.0f)) {
       // A step of no length: the state as it is, to the bit (slang:576-585).
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 0; k < K; ++k) {
         if (live[k]) {
           const int i = gi[k];
           out[i] = rh[k];
@@ -910,9 +919,9 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
       const float sn = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
       // 1. the cells and the halo
 #pragma unroll
-      for (int k = 0; k < 2; ++k)
+      for (int k = 0; k < K; ++k)
         if (live[k])
-          m.cell[warp + 8 * k + 1][cc + 1] =
+          m.cell[warp + kBlkWarps * k + 1][cc + 1] =
               velocities<FIXED>(rh[k], rhu[k], rhv[k], bed[gi[k]], dry);
       if (t < 2 * kBlkW + 2 * kBlkH) {
         int r, c, gy, gx;  // the halo cell's local place and the global cell it reads
@@ -974,7 +983,7 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
       // 2. the faces
       const int nfx = rows * (cols + 1), nfy = (rows + 1) * cols;
       const bool full = cols == kBlkW;
-      for (int q = t; q < nfx + nfy; q += kBlkThreads) {
+      for (int q = t; q < nfx + nfy; q += THREADS) {
         if (q < nfx) {
           const int r = full ? q / (kBlkW + 1) : q / (cols + 1);
           const int f = q - r * (cols + 1);
@@ -997,8 +1006,9 @@ __global__ void __launch_bounds__(kBlkThreads, 4) tick_block_kernel(TickArgs a) 
       const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
                          apply, comp, manning, (flags & 15u) != 0u};
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int r = warp + 8 * k;
+      for (int k = 0; k < K; ++k) {
+        const int r = warp + kBlkWarps * k;
+        if (r >= kBlkH) break;  // a warp past the block's rows (more than 512 threads)
         float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
         if (live[k]) {
           const int i = gi[k];
@@ -1277,22 +1287,24 @@ const void* split_fn(bool fixed, bool manning) {
                  : (const void*)tick_split_kernel<false, false>;
 }
 
+template <int THREADS>
 const void* block_fn(bool fixed, bool manning) {
   if (fixed)
-    return manning ? (const void*)tick_block_kernel<true, true>
-                   : (const void*)tick_block_kernel<true, false>;
-  return manning ? (const void*)tick_block_kernel<false, true>
-                 : (const void*)tick_block_kernel<false, false>;
+    return manning ? (const void*)tick_block_kernel<true, true, THREADS>
+                   : (const void*)tick_block_kernel<true, false, THREADS>;
+  return manning ? (const void*)tick_block_kernel<false, true, THREADS>
+                 : (const void*)tick_block_kernel<false, false, THREADS>;
 }
 
+template <int THREADS>
 cudaError_t block_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
   const size_t smem = sizeof(BlockSmem);
   if (fixed) {
-    if (manning) tick_block_kernel<true, true><<<grid, kBlkThreads, smem, s>>>(a);
-    else tick_block_kernel<true, false><<<grid, kBlkThreads, smem, s>>>(a);
+    if (manning) tick_block_kernel<true, true, THREADS><<<grid, THREADS, smem, s>>>(a);
+    else tick_block_kernel<true, false, THREADS><<<grid, THREADS, smem, s>>>(a);
   } else {
-    if (manning) tick_block_kernel<false, true><<<grid, kBlkThreads, smem, s>>>(a);
-    else tick_block_kernel<false, false><<<grid, kBlkThreads, smem, s>>>(a);
+    if (manning) tick_block_kernel<false, true, THREADS><<<grid, THREADS, smem, s>>>(a);
+    else tick_block_kernel<false, false, THREADS><<<grid, THREADS, smem, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -1362,13 +1374,16 @@ size_t tick_smem_bytes(BlockShape shape) {
     case BlockShape::k32x32: return kWarpsPerCta * WarpMem<32>::kBytes;
     case BlockShape::k32x64: return kWarpsPerCta * WarpMem<64>::kBytes;
     case BlockShape::k32x16s: return kWarpsPerCta * WarpMem<4>::kBytes;
-    case BlockShape::k32x16b: return sizeof(BlockSmem);
+    case BlockShape::k32x16b:
+    case BlockShape::k32x16w: return sizeof(BlockSmem);
   }
   return 0;
 }
 
 int tick_threads(BlockShape shape) {
-  return shape == BlockShape::k32x16b ? kBlkThreads : kCtaThreads;
+  if (shape == BlockShape::k32x16b) return kBlkThreads;
+  if (shape == BlockShape::k32x16w) return kBlkWideThreads;
+  return kCtaThreads;
 }
 
 void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
@@ -1378,7 +1393,8 @@ void block_dims(BlockShape shape, uint32_t& bx, uint32_t& by) {
     case BlockShape::k32x32: by = 32; return;
     case BlockShape::k32x64: by = 64; return;
     case BlockShape::k32x16s:
-    case BlockShape::k32x16b: by = 16; return;
+    case BlockShape::k32x16b:
+    case BlockShape::k32x16w: by = 16; return;
   }
   by = 0;
 }
@@ -1390,7 +1406,8 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning, bool plain) {
     case BlockShape::k32x32: fn = tick_fn<32>(fixed, manning, plain); break;
     case BlockShape::k32x64: fn = tick_fn<64>(fixed, manning, plain); break;
     case BlockShape::k32x16s: fn = split_fn(fixed, manning); break;
-    case BlockShape::k32x16b: fn = block_fn(fixed, manning); break;
+    case BlockShape::k32x16b: fn = block_fn<kBlkThreads>(fixed, manning); break;
+    case BlockShape::k32x16w: fn = block_fn<kBlkWideThreads>(fixed, manning); break;
   }
   const size_t smem = tick_smem_bytes(shape);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
@@ -1409,7 +1426,8 @@ cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain, 
     case BlockShape::k32x32: return tick_launch<32>(fixed, manning, plain, a, grid, s);
     case BlockShape::k32x64: return tick_launch<64>(fixed, manning, plain, a, grid, s);
     case BlockShape::k32x16s: return split_launch(fixed, manning, a, grid, s);
-    case BlockShape::k32x16b: return block_launch(fixed, manning, a, grid, s);
+    case BlockShape::k32x16b: return block_launch<kBlkThreads>(fixed, manning, a, grid, s);
+    case BlockShape::k32x16w: return block_launch<kBlkWideThreads>(fixed, manning, a, grid, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -1419,7 +1437,8 @@ cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaSt
   switch (shape) {
     case BlockShape::k32x16:
     case BlockShape::k32x16s:
-    case BlockShape::k32x16b: return prime_launch<16>(fixed, a, s);
+    case BlockShape::k32x16b:
+    case BlockShape::k32x16w: return prime_launch<16>(fixed, a, s);
     case BlockShape::k32x32: return prime_launch<32>(fixed, a, s);
     case BlockShape::k32x64: return prime_launch<64>(fixed, a, s);
   }

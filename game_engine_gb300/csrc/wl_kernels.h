@@ -26,8 +26,11 @@ struct TickArgs {
 // them; (k32x16s) 32 by 16 split over a CTA's four warps, four rows each, for tiles with too few
 // items to fill the device; or (k32x16b) 32 by 16 by a CTA of 256 threads in three phases through
 // shared memory (cells, then every face on its own thread, then the updates). The batched form's
-// autotuner chooses among all five.
-enum class BlockShape : uint8_t { k32x16 = 0, k32x32 = 1, k32x64 = 2, k32x16s = 3, k32x16b = 4 };
+// autotuner chooses among these five. (k32x16w) is k32x16b by a CTA of 512 threads, which a tile
+// set launches in k32x16b's place when the launch holds no more blocks than the device has SMs.
+enum class BlockShape : uint8_t {
+  k32x16 = 0, k32x32 = 1, k32x64 = 2, k32x16s = 3, k32x16b = 4, k32x16w = 5
+};
 
 size_t tick_smem_bytes(BlockShape shape);
 int tick_threads(BlockShape shape);

@@ -229,7 +229,7 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
     return false;
   }
   for (BlockShape s : {BlockShape::k32x16, BlockShape::k32x32, BlockShape::k32x64,
-                       BlockShape::k32x16s, BlockShape::k32x16b})
+                       BlockShape::k32x16s, BlockShape::k32x16b, BlockShape::k32x16w})
     for (int v = 0; v < 3; ++v)  // Manning's, the plain and the general variant
       if (tick_occupancy(s, fixed_, v == 0, v == 1) <= 0) {
         if (err) *err = "water_live: the tick kernel cannot be resident on this device";
@@ -281,6 +281,7 @@ bool TileSet::layout_items(BlockShape shape, const std::vector<uint32_t>& order,
   if (!check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), err,
              "cudaDeviceGetAttribute"))
     return false;
+  sms_ = sms;
   const int occ = tick_occupancy(shape, fixed_, any_manning(), plain());
   grid_ = std::max(1, std::min<int>(int(n_items_), sms * std::max(1, occ)));
   // The items' tile indices: a separate small allocation, replaced on a reshape.
@@ -331,8 +332,12 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   a.max_dt = max_dt;
   a.go = go;
   const bool manning = any_manning(), plain_set = plain();
+  // The block shape's wide CTA where the launch holds no more blocks than the device has SMs.
+  const BlockShape shape = shape_ == BlockShape::k32x16b && n_items_ <= uint32_t(sms_)
+                               ? BlockShape::k32x16w
+                               : shape_;
   for (uint32_t i = 0; i < count; ++i) {
-    const cudaError_t e = launch_tick(shape_, fixed_, manning, plain_set, a, grid_, s);
+    const cudaError_t e = launch_tick(shape, fixed_, manning, plain_set, a, grid_, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -119,6 +119,7 @@ class TileSet {
   uint32_t* d_item_tile_ = nullptr;  // the tile of each work item (null for one tile)
   uint32_t n_items_ = 0;
   int grid_ = 0;
+  int sms_ = 0;  // the device's SM count
   uint64_t total_cells_ = 0;
   std::vector<uint64_t> first_;  // each tile's first cell in the concatenated arrays
   uint64_t* d_first_ = nullptr;
