@@ -553,6 +553,7 @@ __device__ __forceinline__ void leave(const AdjArgs& a) {
 
 template <int MODE, int H>
 __global__ void __launch_bounds__(kCta, 4) adj_forward_kernel(AdjArgs a) {
+  dependent_grid_start();
   __shared__ float4 side[kWarps][2][H];
   const int warp = threadIdx.x >> 5;
   const uint32_t t = a.t, k = a.every;
@@ -574,6 +575,7 @@ __global__ void __launch_bounds__(kCta, 4) adj_forward_kernel(AdjArgs a) {
 
 template <int H>
 __global__ void __launch_bounds__(kCta, 4) adj_reverse_kernel(AdjArgs a) {
+  dependent_grid_start();
   __shared__ float4 side[kWarps][3][H];
   const int warp = threadIdx.x >> 5;
   const uint32_t t = a.t, k = a.every;
@@ -676,15 +678,11 @@ cudaError_t launch_adj_copy_in(const TileDesc* set_tiles, const AdjTile* tiles, 
   return cudaGetLastError();
 }
 
+// The sweep's marches are launched as programmatic dependents (dependent_grid_start).
 cudaError_t launch_adj_forward(int mode, int rows, const AdjArgs& a, int grid, cudaStream_t s) {
-  if (rows == 4) {
-    if (mode == 0) adj_forward_kernel<0, 4><<<grid, kCta, 0, s>>>(a);
-    else adj_forward_kernel<1, 4><<<grid, kCta, 0, s>>>(a);
-  } else {
-    if (mode == 0) adj_forward_kernel<0, 16><<<grid, kCta, 0, s>>>(a);
-    else adj_forward_kernel<1, 16><<<grid, kCta, 0, s>>>(a);
-  }
-  return cudaGetLastError();
+  void (*k)(AdjArgs) = rows == 4 ? (mode == 0 ? adj_forward_kernel<0, 4> : adj_forward_kernel<1, 4>)
+                                 : (mode == 0 ? adj_forward_kernel<0, 16> : adj_forward_kernel<1, 16>);
+  return launch_dependent(k, dim3(unsigned(grid)), dim3(kCta), 0, s, a);
 }
 
 cudaError_t launch_adj_check(const AdjArgs& a, uint32_t count, cudaStream_t s) {
@@ -698,9 +696,8 @@ cudaError_t launch_adj_seed(const AdjArgs& a, uint32_t count, cudaStream_t s) {
 }
 
 cudaError_t launch_adj_reverse(int rows, const AdjArgs& a, int grid, cudaStream_t s) {
-  if (rows == 4) adj_reverse_kernel<4><<<grid, kCta, 0, s>>>(a);
-  else adj_reverse_kernel<16><<<grid, kCta, 0, s>>>(a);
-  return cudaGetLastError();
+  void (*k)(AdjArgs) = rows == 4 ? adj_reverse_kernel<4> : adj_reverse_kernel<16>;
+  return launch_dependent(k, dim3(unsigned(grid)), dim3(kCta), 0, s, a);
 }
 
 // ---- the sweep -------------------------------------------------------------------------------

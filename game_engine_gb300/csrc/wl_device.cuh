@@ -95,6 +95,35 @@ struct WorkCtl {
   uint32_t pad[2];
 };
 
+// ---- dependent launches ---------------------------------------------------------------------
+//
+// The tick, the queue's slot and the adjoint's sweeps are launched as programmatic dependents of
+// the launch before them on their stream: their CTAs may be scheduled while that grid's last CTAs
+// finish. griddepcontrol.wait returns once the grid before has completed and its writes are
+// visible, so nothing such a kernel reads is read before it; the kernel then lets the grid after it
+// be scheduled, which waits the same way. At most two such grids are resident at once, and a
+// launch before which nothing signals (an ordinary kernel, a copy) is waited for in full.
+__device__ __forceinline__ void dependent_grid_start() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... Params, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem,
+                                    cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // ---- the arithmetic (water_step.slang:105-191) -------------------------------------------------
 
 __device__ __forceinline__ float max2(float a, float b) { return a > b ? a : b; }

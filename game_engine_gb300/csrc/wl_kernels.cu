@@ -70,16 +70,6 @@ __device__ __forceinline__ uint32_t item_tile_of(const uint32_t* item_tile, uint
   return item_tile == nullptr ? 0u : item_tile[item];
 }
 
-// A tick grid is launched as a programmatic dependent of the launch before it on its stream: its
-// CTAs may be scheduled while that grid's last CTAs finish. griddepcontrol.wait returns once the
-// grid before has completed and its writes are visible, so nothing a tick reads is read before
-// it. The tick then lets the grid after it be scheduled (that grid waits the same way): at most
-// two tick grids are resident at once, and a launch before which nothing signals (an ordinary
-// kernel, a copy) is waited for in full.
-__device__ __forceinline__ void tick_grid_start() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
 
 // ---- the ledger ---------------------------------------------------------------------------
 
@@ -675,7 +665,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
 // which then fits 80 registers: six CTAs an SM instead of five.
 template <bool FIXED, bool MANNING, int H, bool PLAIN>
 __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickArgs a) {
-  tick_grid_start();
+  dependent_grid_start();
   if (a.go != nullptr && *a.go == 0u) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const WarpMem<H> wm = warp_mem<H>(warp);
@@ -738,7 +728,7 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
 // The items are the 32 x 16 shape's.
 template <bool FIXED, bool MANNING>
 __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) {
-  tick_grid_start();
+  dependent_grid_start();
   if (a.go != nullptr && *a.go == 0u) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const WarpMem<4> wm = warp_mem<4>(warp);
@@ -840,7 +830,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
                 "fold_block takes a thread a virtual lane");
   static_assert(THREADS >= 2 * kBlkW + 2 * kBlkH, "a thread a halo cell");
   constexpr int kBlkWarps = THREADS / 32;
-  tick_grid_start();
+  dependent_grid_start();
   if (a.go != nullptr && *a.go == 0u) return;
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
@@ -1301,22 +1291,6 @@ const void* split_fn(bool fixed, bool manning) {
                  : (const void*)tick_split_kernel<false, false>;
 }
 
-// A tick launch: a programmatic dependent of the stream's launch before it (tick_grid_start).
-cudaError_t launch_dependent(void (*kernel)(TickArgs), int grid, int threads, size_t smem,
-                             cudaStream_t s, const TickArgs& a) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(unsigned(grid));
-  cfg.blockDim = dim3(unsigned(threads));
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, a);
-}
-
 template <int THREADS>
 const void* block_fn(bool fixed, bool manning) {
   if (fixed)
@@ -1332,14 +1306,14 @@ cudaError_t block_launch(bool fixed, bool manning, const TickArgs& a, int grid, 
       fixed ? (manning ? tick_block_kernel<true, true, THREADS> : tick_block_kernel<true, false, THREADS>)
             : (manning ? tick_block_kernel<false, true, THREADS>
                        : tick_block_kernel<false, false, THREADS>);
-  return launch_dependent(k, grid, THREADS, sizeof(BlockSmem), s, a);
+  return launch_dependent(k, dim3(grid), dim3(THREADS), sizeof(BlockSmem), s, a);
 }
 
 cudaError_t split_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
   const size_t smem = kWarpsPerCta * WarpMem<4>::kBytes;
   void (*k)(TickArgs) = fixed ? (manning ? tick_split_kernel<true, true> : tick_split_kernel<true, false>)
                               : (manning ? tick_split_kernel<false, true> : tick_split_kernel<false, false>);
-  return launch_dependent(k, grid, kCtaThreads, smem, s, a);
+  return launch_dependent(k, dim3(grid), dim3(kCtaThreads), smem, s, a);
 }
 
 // The march's variants: Manning's, the plain one (where `plain` and no Manning), the general one.
@@ -1364,7 +1338,8 @@ cudaError_t tick_launch(bool fixed, bool manning, bool plain, const TickArgs& a,
             : (manning ? tick_kernel<false, true, H, false>
                        : plain ? tick_kernel<false, false, H, true>
                                : tick_kernel<false, false, H, false>);
-  return launch_dependent(k, grid, kCtaThreads, kWarpsPerCta * WarpMem<H>::kBytes, s, a);
+  return launch_dependent(k, dim3(grid), dim3(kCtaThreads), kWarpsPerCta * WarpMem<H>::kBytes, s,
+                          a);
 }
 
 template <int H>

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
     QueueCtl* q, const QueueRecord* ring, uint32_t records, wl_landed* landed,
     const TileDesc* tiles, uint32_t n_tiles, uint32_t* seen, int may_begin,
     const QueueEvent* events, uint32_t max_events, const float* arena, uint32_t arena_values) {
+  dependent_grid_start();  // a slot between two ticks is a dependent launch like them
   __shared__ uint32_t s_left, s_stepped, s_min, s_max, s_begin, s_apply;
   __shared__ float s_len;
   const uint32_t t = threadIdx.x;
@@ -352,10 +353,10 @@ cudaError_t TickQueue::enqueue(cudaStream_t s, uint32_t slots) {
   const float inf = std::numeric_limits<float>::infinity();
   const TileDesc* tiles = set_->device_descs();
   for (uint32_t k = 0; k < slots; ++k) {
-    queue_slot_kernel<<<1, kApplyThreads, 0, s>>>(d_ctl_, d_ring_, records_, d_landed_, tiles,
-                                                   tiles_, d_seen_, 1, d_events_, max_events_,
-                                                   d_arena_, arena_);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_dependent(queue_slot_kernel, dim3(1), dim3(kApplyThreads), 0, s, d_ctl_,
+                                     (const QueueRecord*)d_ring_, records_, d_landed_, tiles,
+                                     tiles_, d_seen_, 1, (const QueueEvent*)d_events_, max_events_,
+                                     (const float*)d_arena_, arena_);
     if (e != cudaSuccess) return e;
     e = set_->enqueue_ticks(s, 1, inf, &d_ctl_->go);
     if (e != cudaSuccess) return e;
