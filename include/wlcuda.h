@@ -151,7 +151,11 @@ int wl_set_source(wl_step* step, const double* source_m_per_s, size_t n, uint32_
  * the device, so a captured graph of these launches may be replayed any number of times. The
  * kernel each launch runs is chosen when it is enqueued, from the step's flags (Manning on, the
  * compensated source, open edges): a graph captured before wl_set_manning or wl_set_source changes
- * those must be captured again. */
+ * those must be captured again. Each tick is launched as a programmatic dependent of the launch
+ * before it on the stream (it reads nothing before that launch has completed) and lets the launch
+ * after it be scheduled at its start: a caller's own kernel launched next with programmatic stream
+ * serialization must wait on its grid dependency (cudaGridDependencySynchronize) before it reads
+ * the state; any other launch or copy after the ticks waits for them in full. */
 int wl_enqueue_steps(wl_step* step, wl_stream stream, uint32_t count, float max_dt);
 /* DeviceStep::run_steps (water_live.cpp:570-574): enqueued on the step's own stream and waited for. */
 int wl_run_steps(wl_step* step, uint32_t count, float max_dt, char* err, size_t err_len);
