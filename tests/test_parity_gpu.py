@@ -79,6 +79,22 @@ def test_odd_sizes_and_partial_blocks(gpu, nx, ny, rows):
     assert_same(dev, ref, f"{nx}x{ny}")
 
 
+@pytest.mark.parametrize("edges", [0, 9])
+def test_block_shape_on_a_tile_of_more_blocks_than_sms(gpu, edges):
+    """The three-phase block shape in its 256-thread CTA (a 700 x 300 tile is 22 x 19 = 418 blocks,
+    more than the device has SMs; smaller launches take the 512-thread CTA, which the odd sizes
+    above cover): rain with sinks, 40 ticks against the oracle."""
+    nx, ny = 700, 300
+    x, y = cases.grid_xy(nx, ny)
+    bed = (cases.mix(x, y) % 1000).astype(float) / 400.0
+    h = np.maximum(2.0 - bed, 0.0) + (cases.mix(y, x) % 5 == 0) * 0.3
+    source = np.where(cases.mix(x + np.uint64(7), y) % 13 == 0, -2e-3, 5e-4)
+    c = dict(nx=nx, ny=ny, cell_m=1.0, bed=bed, h=h, source=source, open_edges=edges)
+    dev, ref = make_pair(c, rows=1)
+    run_both(dev, ref, steps=40)
+    assert_same(dev, ref, f"700x300 edges {edges}")
+
+
 @pytest.mark.parametrize("every,compensate", [(1, False), (8, False), (64, False), (1, True)])
 def test_slow_sink_forms(gpu, every, compensate):
     # device_tests.cpp:743-787 in small: a pond losing 3.7e-6 m/s at 1/60 s steps.
