@@ -90,9 +90,10 @@ struct TileDesc {
 
 // A launch's dynamic work counter: CTAs take work items in order; the last CTA to leave resets it.
 struct WorkCtl {
-  uint32_t next;
-  uint32_t exited;
-  uint32_t pad[2];
+  uint32_t next;    // whole items dealt
+  uint32_t exited;  // warps (or CTAs) that left
+  uint32_t tail;    // the 32 x 16 march's last items dealt, a CTA at a time
+  uint32_t pad;
 };
 
 // ---- dependent launches ---------------------------------------------------------------------

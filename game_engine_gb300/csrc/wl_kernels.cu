@@ -660,6 +660,79 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   if (SPLIT) split_partials(ring, ring_row0, rows, ga, gb, opn_seen, rnd_seen, s_ab, s_need);
 }
 
+// The 32 x 16 march's last items, n_whole .. n_items - 1 (fewer than the launch's warps): a CTA
+// at a time, its four warps four rows each (the split march, the item's volumes in the CTA's
+// shared ring, the records by warp 0 after a barrier), so that the launch's last round is a
+// quarter of an item long instead of a whole one. The CTA's warps meet here when the whole items
+// run out. Out of line: the whole-item march keeps its registers.
+template <bool FIXED, bool MANNING, bool PLAIN>
+__device__ __noinline__ void tail_items(TickArgs a, const WarpMem<16> wm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ uint32_t s_item, s_need;
+  __shared__ uint32_t s_ab[4];
+  float* ring = warp_mem<16>(0).ring;     // the item's 16 rows of volumes
+  float* scratch = warp_mem<16>(1).ring;  // the ledger fold's slots
+  WarpMem<4> w4;
+  w4.west = wm.west;
+  w4.east = wm.east;
+  w4.ring = wm.ring;
+  __syncthreads();  // every warp's whole items are done: warp 0's ring is the CTA's
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = atomicAdd(&a.work->tail, 1u);
+      s_need = 0u;
+    }
+    if (threadIdx.x < 4) s_ab[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t item = a.n_whole + s_item;
+    if (item >= a.n_items) break;
+    const uint32_t tile = item_tile_of(a.item_tile, item);
+    const TileDesc& T = a.tiles[tile];
+    const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
+    const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+    const TileCtl* ctl = T.ctl;
+    Item it;
+    it.cur = ctl->cur;
+    it.rec = ctl->rec;
+    const float pa = __uint_as_float(ctl->max_a[it.rec]);
+    const float pb = __uint_as_float(ctl->max_b[it.rec]);
+    it.dt = choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[it.rec].remaining_s);
+    if (a.go != nullptr && !(ctl->ledger[it.rec].remaining_s > 0.0f)) {  // a landed tile
+      __syncthreads();
+      continue;
+    }
+    const bool src = (T.flags & kFlagSource) != 0u;
+    const bool on = src && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
+    it.apply_source = on ? 1u : 0u;
+    it.scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
+    it.X0 = int(bx) * kStrip;
+    const int Y0 = int(by) * 16;
+    it.Y0 = Y0 + 4 * warp;
+    if (local == 0u && warp == 1) {
+      fold_warp(T.rec[it.rec], T.groups_x * T.groups_y, scratch);
+      if (lane == 0) {
+        LedgerBits l = ctl->ledger[it.rec];
+        ledger_update<FIXED>(l, scratch[0], scratch[kGroupCells], scratch[2 * kGroupCells], pa,
+                             pb, T.cfl, T.cell_m, a.max_dt);
+        T.ctl->ledger[it.rec ^ 1u] = l;
+      }
+      __syncwarp();
+    }
+    uint32_t ia = 0u, ib = 0u;
+    march<FIXED, MANNING, 4, true, PLAIN>(T, it, w4, ring, 4 * warp, s_ab, &s_need, ia, ib);
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t ga = s_ab[lane < 16 ? 0 : 2], gb = s_ab[lane < 16 ? 1 : 3];
+      const uint32_t need = s_need;
+      group_records(T.groups_x, T.groups_y, T.rec[it.rec ^ 1u], it.X0, Y0 / 16, ga, gb, ring,
+                    it.dt > 0.0f && it.apply_source != 0u, (need & 1u) != 0u, (need & 2u) != 0u,
+                    ia, ib);
+      if (lane == 0) finish_item(T, it.rec, ia, ib, true);
+    }
+    __syncthreads();
+  }
+}
+
 // The persistent tick: every work item of every tile, one tick. PLAIN (no tile holds a flag of
 // kFlagsNotPlain) compiles the open edges, the compensated source and Manning out of the march,
 // which then fits 80 registers: six CTAs an SM instead of five.
@@ -673,7 +746,7 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
     uint32_t item = 0u;
     if (lane == 0) item = atomicAdd(&a.work->next, 1u);
     item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= a.n_items) break;
+    if (item >= a.n_whole) break;
     const uint32_t tile = item_tile_of(a.item_tile, item);
     const TileDesc& T = a.tiles[tile];
     const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
@@ -713,10 +786,14 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
     if (lane == 0) finish_item(T, T.ctl->rec, ia, ib, true);
     __syncwarp();
   }
+  if constexpr (H == 16) {
+    if (a.n_whole < a.n_items) tail_items<FIXED, MANNING, PLAIN>(a, wm);  // the same in every CTA
+  }
   if (lane == 0) {
     __threadfence();
     if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x * kWarpsPerCta) {
       a.work->next = 0u;
+      a.work->tail = 0u;
       a.work->exited = 0u;
       __threadfence();
     }
@@ -1411,8 +1488,15 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning, bool plain) {
   return blocks;
 }
 
-cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain, const TickArgs& a,
-                        int grid, cudaStream_t s) {
+cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain,
+                        const TickArgs& args, int grid, cudaStream_t s) {
+  TickArgs a = args;
+  a.n_whole = a.n_items;
+  if (shape == BlockShape::k32x16 && grid > 0) {
+    // Whole rounds of items a warp each; the remainder (fewer than the warps) a CTA each.
+    const uint32_t warps = uint32_t(grid) * uint32_t(kWarpsPerCta);
+    if (a.n_items > warps) a.n_whole = a.n_items - a.n_items % warps;
+  }
   switch (shape) {
     case BlockShape::k32x16: return tick_launch<16>(fixed, manning, plain, a, grid, s);
     case BlockShape::k32x32: return tick_launch<32>(fixed, manning, plain, a, grid, s);

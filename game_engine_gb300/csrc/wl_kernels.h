@@ -20,6 +20,9 @@ struct TickArgs {
   uint32_t n_items;
   float max_dt;
   const uint32_t* go = nullptr;
+  // Set by launch_tick: the 32 x 16 march takes items 0 .. n_whole - 1 a warp each and the rest
+  // (fewer than its warps) a CTA each, four rows a warp.
+  uint32_t n_whole = 0;
 };
 
 // The block of cells one work item steps: 32 columns by 16, 32 or 64 rows, one warp marching
