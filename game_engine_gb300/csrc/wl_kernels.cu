@@ -70,6 +70,16 @@ __device__ __forceinline__ uint32_t item_tile_of(const uint32_t* item_tile, uint
   return item_tile == nullptr ? 0u : item_tile[item];
 }
 
+// The next item of one of a persistent tick's `slots` takers (CTAs or warps), the one numbered
+// `own`: its own number first, then slots + the work counter's next value. A launch of no more
+// takers than items (a small tile's) reads no counter, and leaves it as it found it.
+__device__ __forceinline__ uint32_t take_item(WorkCtl* w, bool first, uint32_t own, uint32_t slots,
+                                              uint32_t n) {
+  if (first) return own;
+  if (slots >= n) return n;
+  return slots + atomicAdd(&w->next, 1u);
+}
+
 
 // ---- the ledger ---------------------------------------------------------------------------
 
@@ -742,9 +752,10 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
   if (a.go != nullptr && *a.go == 0u) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const WarpMem<H> wm = warp_mem<H>(warp);
-  for (;;) {
+  const uint32_t slots = gridDim.x * kWarpsPerCta, own = blockIdx.x * kWarpsPerCta + warp;
+  for (bool first = true;; first = false) {
     uint32_t item = 0u;
-    if (lane == 0) item = atomicAdd(&a.work->next, 1u);
+    if (lane == 0) item = take_item(a.work, first, own, slots, a.n_whole);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= a.n_whole) break;
     const uint32_t tile = item_tile_of(a.item_tile, item);
@@ -789,9 +800,9 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
   if constexpr (H == 16) {
     if (a.n_whole < a.n_items) tail_items<FIXED, MANNING, PLAIN>(a, wm);  // the same in every CTA
   }
-  if (lane == 0) {
+  if (lane == 0 && slots < a.n_items) {  // the counters were read: the last warp out resets them
     __threadfence();
-    if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x * kWarpsPerCta) {
+    if (atomicAdd(&a.work->exited, 1u) + 1u == slots) {
       a.work->next = 0u;
       a.work->tail = 0u;
       a.work->exited = 0u;
@@ -813,9 +824,9 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
   float* scratch = warp_mem<4>(1).ring;  // the ledger fold's slots
   __shared__ uint32_t s_item, s_need;
   __shared__ uint32_t s_ab[4];
-  for (;;) {
+  for (bool first = true;; first = false) {
     if (threadIdx.x == 0) {
-      s_item = atomicAdd(&a.work->next, 1u);
+      s_item = take_item(a.work, first, blockIdx.x, gridDim.x, a.n_items);
       s_need = 0u;
     }
     if (threadIdx.x < 4) s_ab[threadIdx.x] = 0u;
@@ -867,7 +878,7 @@ __global__ void __launch_bounds__(kCtaThreads, 5) tick_split_kernel(TickArgs a) 
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && gridDim.x < a.n_items) {  // the counter was read
     __threadfence();
     if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x) {
       a.work->next = 0u;
@@ -912,9 +923,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  for (;;) {
+  for (bool first = true;; first = false) {
     if (t == 0) {
-      m.item = atomicAdd(&a.work->next, 1u);
+      m.item = take_item(a.work, first, blockIdx.x, gridDim.x, a.n_items);
       m.need = 0u;
     }
     if (t < 4) m.ab[t] = 0u;
@@ -1141,7 +1152,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     }
     __syncthreads();
   }
-  if (t == 0) {
+  if (t == 0 && gridDim.x < a.n_items) {  // the counter was read
     __threadfence();
     if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x) {
       a.work->next = 0u;
