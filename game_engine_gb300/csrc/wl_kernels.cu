@@ -200,13 +200,14 @@ __device__ void ledger_update(LedgerBits& l, float src, float opn, float rnd, fl
 // read by the next launch, and the flip reads only fields no other item writes. Every other item
 // of the tile has read slot `rec` (its step's length) before its count, so the last item may clear
 // it. A tick also flips the copy and moves the source's clock; a prime flips only the records.
+// `extra` counts a CTA that folded the ledger apart from the items (1) or none (0).
 __device__ void finish_item(const TileDesc& T, uint32_t rec, uint32_t amax, uint32_t bmax,
-                            bool tick) {
+                            bool tick, uint32_t extra = 0u) {
   TileCtl* ctl = T.ctl;
   atomicMax(&ctl->max_a[rec ^ 1u], amax);
   atomicMax(&ctl->max_b[rec ^ 1u], bmax);
   const uint32_t d = atomicAdd(&ctl->done, 1u);
-  if (d + 1u != T.items) return;
+  if (d + 1u != T.items + extra) return;
   volatile TileCtl* v = ctl;
   v->max_a[rec] = 0u;
   v->max_b[rec] = 0u;
@@ -923,6 +924,25 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (a.fold_apart != 0u && blockIdx.x + 1u == gridDim.x) {
+    // The tile's dt_main fold (slang:417-478) on a CTA of its own, beside the items: a single
+    // tile's launch of fewer items than SMs, whose item 0 would otherwise fold before it steps. It
+    // counts as one more item, so the flip waits for its read of slot `rec`.
+    const TileDesc& T = a.tiles[0];
+    const TileCtl* ctl = T.ctl;
+    const uint32_t rec = ctl->rec;
+    if (a.go != nullptr && !(ctl->ledger[rec].remaining_s > 0.0f)) return;  // a landed tile
+    const float pa = __uint_as_float(ctl->max_a[rec]), pb = __uint_as_float(ctl->max_b[rec]);
+    fold_block(T.rec[rec], T.groups_x * T.groups_y, m.fold);
+    if (t == 0) {
+      LedgerBits l = ctl->ledger[rec];
+      ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
+                           T.cfl, T.cell_m, a.max_dt);
+      T.ctl->ledger[rec ^ 1u] = l;
+      finish_item(T, rec, 0u, 0u, true, 1u);
+    }
+    return;
+  }
   for (bool first = true;; first = false) {
     if (t == 0) {
       m.item = take_item(a.work, first, blockIdx.x, gridDim.x, a.n_items);
@@ -949,7 +969,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
     const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
-    if (local == 0u) {
+    if (local == 0u && a.fold_apart == 0u) {
       // dt_main's fold of the last update's records (slang:417-478) by the whole CTA, a thread a
       // virtual lane, into the ledger's next slot.
       fold_block(T.rec[rec], T.groups_x * T.groups_y, m.fold);
@@ -1148,7 +1168,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
       group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[lane < 16 ? 0 : 2],
                     m.ab[lane < 16 ? 1 : 3], m.ring, dt > 0.0f && apply, (need & 1u) != 0u,
                     (need & 2u) != 0u, ia, ib);
-      if (lane == 0) finish_item(T, rec, ia, ib, true);
+      if (lane == 0) finish_item(T, rec, ia, ib, true, a.fold_apart);
     }
     __syncthreads();
   }

@@ -23,6 +23,9 @@ struct TickArgs {
   // Set by launch_tick: the 32 x 16 march takes items 0 .. n_whole - 1 a warp each and the rest
   // (fewer than its warps) a CTA each, four rows a warp.
   uint32_t n_whole = 0;
+  // The block shape, one tile: the grid's last CTA folds the tile's ledger instead of item 0
+  // (the launch holds one CTA more than items).
+  uint32_t fold_apart = 0;
 };
 
 // The block of cells one work item steps: 32 columns by 16, 32 or 64 rows, one warp marching

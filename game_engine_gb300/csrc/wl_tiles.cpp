@@ -332,12 +332,17 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   a.max_dt = max_dt;
   a.go = go;
   const bool manning = any_manning(), plain_set = plain();
-  // The block shape's wide CTA where the launch holds no more blocks than the device has SMs.
-  const BlockShape shape = shape_ == BlockShape::k32x16b && n_items_ <= uint32_t(sms_)
-                               ? BlockShape::k32x16w
-                               : shape_;
+  // The block shape's wide CTA where the launch holds no more blocks than the device has SMs; for
+  // one tile, one CTA more folds its ledger beside the items.
+  const bool wide = shape_ == BlockShape::k32x16b && n_items_ <= uint32_t(sms_);
+  const BlockShape shape = wide ? BlockShape::k32x16w : shape_;
+  int grid = grid_;
+  if (wide && d_item_tile_ == nullptr) {
+    a.fold_apart = 1u;
+    grid = int(n_items_) + 1;
+  }
   for (uint32_t i = 0; i < count; ++i) {
-    const cudaError_t e = launch_tick(shape, fixed_, manning, plain_set, a, grid_, s);
+    const cudaError_t e = launch_tick(shape, fixed_, manning, plain_set, a, grid, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
