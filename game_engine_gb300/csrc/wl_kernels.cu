@@ -991,7 +991,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     // The cells this thread updates: rows warp + kBlkWarps k of column t & 31.
     constexpr int K = (kBlkH + kBlkWarps - 1) / kBlkWarps;
     const int cc = lane;
-    float rh[K], rhu[K], rhv[K];
+    float rh[K], rhu[K], rhv[K], rsrc[K];
     bool live[K];
     int gi[K];
 #pragma unroll
@@ -999,11 +999,14 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
       const int r = warp + kBlkWarps * k;
       live[k] = r < rows && cc < cols;
       gi[k] = (Y0 + r) * nx + X0 + cc;
-      rh[k] = rhu[k] = rhv[k] = 0.0f;
+      rh[k] = rhu[k] = rhv[k] = rsrc[k] = 0.0f;
       if (live[k]) {
         rh[k] = in[gi[k]];
         rhu[k] = in[n + gi[k]];
         rhv[k] = in[2 * n + gi[k]];
+        // A thread of one cell loads its source with its state, not after the barriers (two
+        // cells' worth would cost the 256-thread CTA spills).
+        if (K == 1 && apply) rsrc[k] = T.source[gi[k]];
       }
     }
     uint32_t ga = 0u, gb = 0u;
@@ -1126,7 +1129,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
           const int i = gi[k];
           float h, mu, mv, residual;
           update_cell<FIXED>(uc, m.cell[r + 1][cc + 1], rhu[k], rhv[k],
-                             apply ? T.source[i] : 0.0f, comp ? in[3 * n + i] : 0.0f,
+                             K == 1 ? rsrc[k] : (apply ? T.source[i] : 0.0f),
+                             comp ? in[3 * n + i] : 0.0f,
                              manning ? T.manning[i] : 0.0f, m.fx[r][cc], m.fx[r][cc + 1],
                              m.fy[r][cc], m.fy[r + 1][cc], X0 + cc, Y0 + r, h, mu, mv, residual,
                              csrc, copn, crnd);
