@@ -919,6 +919,13 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
                 "fold_block takes a thread a virtual lane");
   static_assert(THREADS >= 2 * kBlkW + 2 * kBlkH, "a thread a halo cell");
   constexpr int kBlkWarps = THREADS / 32;
+  // The first item's tile descriptor into L1 while the grid before finishes: no tick or queue
+  // slot writes a descriptor (only the host's uploads do, and a copy ends a dependent launch's
+  // overlap), so it is the same before the wait as after it.
+  if (threadIdx.x == 0 && blockIdx.x < a.n_items) {
+    const TileDesc* d = a.tiles + item_tile_of(a.item_tile, blockIdx.x);
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(d));
+  }
   dependent_grid_start();
   if (a.go != nullptr && *a.go == 0u) return;
   extern __shared__ float4 smem_raw[];
