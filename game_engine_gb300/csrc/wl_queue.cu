@@ -46,10 +46,6 @@ __device__ void land(QueueCtl* q, const LedgerBits& l, wl_landed* landed, uint32
   q->active = 0u;
 }
 
-__device__ __forceinline__ const LedgerBits& current(const TileDesc& T) {
-  return T.ctl->ledger[T.ctl->rec];
-}
-
 // A slot's first launch, one CTA over the queue's tiles (a step is a set of one):
 //   1. the last slot's effects: a tile whose step count moved took a sub-step (its length into
 //      the tick's shortest and longest), the events the last slot applied are released, and the
@@ -64,10 +60,13 @@ __global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
     QueueCtl* q, const QueueRecord* ring, uint32_t records, wl_landed* landed,
     const TileDesc* tiles, uint32_t n_tiles, uint32_t* seen, int may_begin,
     const QueueEvent* events, uint32_t max_events, const float* arena, uint32_t arena_values) {
+  const uint32_t t = threadIdx.x;
+  // This thread's first tile descriptor into L1 while the grid before finishes: events change the
+  // planes' values, never a descriptor, so it is the same before the wait as after it.
+  if (t < n_tiles) asm volatile("prefetch.global.L1 [%0];" ::"l"(tiles + t));
   dependent_grid_start();  // a slot between two ticks is a dependent launch like them
   __shared__ uint32_t s_left, s_stepped, s_min, s_max, s_begin, s_apply;
   __shared__ float s_len;
-  const uint32_t t = threadIdx.x;
   if (t == 0) {
     s_left = 0u;
     s_stepped = 0u;
@@ -76,8 +75,18 @@ __global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
   }
   __syncthreads();
   uint32_t left = 0u, stepped = 0u, lo = 0x7f800000u, hi = 0u;
+  // This thread's first tile's control block and record slot, kept for the begin below (no tick
+  // runs while a slot does, so neither moves).
+  TileCtl* ctl0 = nullptr;
+  uint32_t rec0 = 0u;
   for (uint32_t k = t; k < n_tiles; k += blockDim.x) {
-    const LedgerBits& l = current(tiles[k]);
+    TileCtl* c = tiles[k].ctl;
+    const uint32_t rec = c->rec;
+    if (k == t) {
+      ctl0 = c;
+      rec0 = rec;
+    }
+    const LedgerBits& l = c->ledger[rec];
     if (l.steps != seen[k]) {
       seen[k] = l.steps;
       stepped = 1u;
@@ -104,7 +113,7 @@ __global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
       q->shortest = fminf(q->shortest, __uint_as_float(s_min));
       q->longest = fmaxf(q->longest, __uint_as_float(s_max));
     }
-    if (q->active != 0u && s_left == 0u) land(q, current(tiles[0]), landed, records);
+    if (q->active != 0u && s_left == 0u) land(q, ctl0->ledger[rec0], landed, records);
     s_begin = 0u;
     const uint32_t head = *static_cast<volatile uint32_t*>(&q->head);  // the host's word
     if (may_begin != 0 && q->active == 0u && q->begun != head) {
@@ -127,12 +136,16 @@ __global__ void __launch_bounds__(kApplyThreads) queue_slot_kernel(
   __syncthreads();
   if (s_begin != 0u) {
     for (uint32_t k = t; k < n_tiles; k += blockDim.x) {
-      TileCtl* c = tiles[k].ctl;
-      c->ledger[c->rec].remaining_s = s_len;
+      if (k == t) {
+        ctl0->ledger[rec0].remaining_s = s_len;
+      } else {
+        TileCtl* c = tiles[k].ctl;
+        c->ledger[c->rec].remaining_s = s_len;
+      }
     }
     __syncthreads();
     // A tick of no length lands now; its events are applied below all the same.
-    if (t == 0 && !(s_len > 0.0f)) land(q, current(tiles[0]), landed, records);
+    if (t == 0 && !(s_len > 0.0f)) land(q, ctl0->ledger[rec0], landed, records);
   }
   if (t == 0) q->go = q->active;
   if (s_apply == 0u) return;
