@@ -524,11 +524,20 @@ struct ItemPos {
 };
 
 template <int H>
-__device__ __forceinline__ bool next_item(const AdjArgs& a, ItemPos& p) {
+// A warp's next item: its own number first, then the warps' count + the work counter's next
+// value; a launch of no more warps than items reads no counter.
+__device__ __forceinline__ bool next_item(const AdjArgs& a, ItemPos& p, bool first) {
   const int lane = threadIdx.x & 31;
+  const uint32_t slots = gridDim.x * kWarps;
   uint32_t item = 0u;
-  if (lane == 0) item = atomicAdd(&a.work->next, 1u);
-  item = __shfl_sync(kFull, item, 0);
+  if (first) {
+    item = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  } else if (slots >= a.n_items) {
+    item = a.n_items;
+  } else {
+    if (lane == 0) item = slots + atomicAdd(&a.work->next, 1u);
+    item = __shfl_sync(kFull, item, 0);
+  }
   if (item >= a.n_items) return false;
   const AdjTile& A = a.tiles[tile_of_item(a.item_tile, item)];
   const uint32_t local = item - A.item_base;
@@ -541,7 +550,7 @@ __device__ __forceinline__ bool next_item(const AdjArgs& a, ItemPos& p) {
 }
 
 __device__ __forceinline__ void leave(const AdjArgs& a) {
-  if ((threadIdx.x & 31) == 0) {
+  if ((threadIdx.x & 31) == 0 && gridDim.x * kWarps < a.n_items) {  // the counter was read
     __threadfence();
     if (atomicAdd(&a.work->exited, 1u) + 1u == gridDim.x * kWarps) {
       a.work->next = 0u;
@@ -560,7 +569,7 @@ __global__ void __launch_bounds__(kCta, 4) adj_forward_kernel(AdjArgs a) {
   const uint32_t c = t / k, j = t - c * k;
   const uint32_t seg_end = min((c + 1u) * k, a.ticks);
   ItemPos p;
-  while (next_item<H>(a, p)) {
+  for (bool first = true; next_item<H>(a, p, first); first = false) {
     const AdjTile& A = *p.A;
     const size_t n3 = 3 * size_t(A.nx) * A.ny;
     const float* in = state_of(A, t, k, n3);
@@ -580,7 +589,7 @@ __global__ void __launch_bounds__(kCta, 4) adj_reverse_kernel(AdjArgs a) {
   const int warp = threadIdx.x >> 5;
   const uint32_t t = a.t, k = a.every;
   ItemPos p;
-  while (next_item<H>(a, p)) {
+  for (bool first = true; next_item<H>(a, p, first); first = false) {
     const AdjTile& A = *p.A;
     const size_t n3 = 3 * size_t(A.nx) * A.ny;
     const float* U = state_of(A, t, k, n3);
