@@ -561,7 +561,9 @@ __device__ __forceinline__ void leave(const AdjArgs& a) {
 }
 
 template <int MODE, int H>
-__global__ void __launch_bounds__(kCta, 4) adj_forward_kernel(AdjArgs a) {
+// 16-row items (a sweep with items enough for every warp) at 80 registers and six CTAs an SM;
+// 4-row items (a small tile, one item a warp) at the registers that keep a warp's chain short.
+__global__ void __launch_bounds__(kCta, H == 16 ? 6 : 4) adj_forward_kernel(AdjArgs a) {
   dependent_grid_start();
   __shared__ float4 side[kWarps][2][H];
   const int warp = threadIdx.x >> 5;
@@ -665,21 +667,25 @@ __global__ void adj_seed_kernel(AdjArgs a) {
 // ---- launchers -------------------------------------------------------------------------------
 
 template <int H>
-int occupancy_of() {
-  int a = 0, b = 0, c = 0;
+int occupancy_of(bool reverse) {
+  int a = 0, b = 0;
+  if (reverse)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, adj_reverse_kernel<H>, kCta, 0) ==
+                   cudaSuccess
+               ? a
+               : 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, adj_forward_kernel<0, H>, kCta, 0) !=
       cudaSuccess)
     return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, adj_forward_kernel<1, H>, kCta, 0) !=
       cudaSuccess)
     return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, adj_reverse_kernel<H>, kCta, 0) !=
-      cudaSuccess)
-    return 0;
-  return std::min(a, std::min(b, c));
+  return std::min(a, b);
 }
 
-int adj_occupancy(int rows) { return rows == 4 ? occupancy_of<4>() : occupancy_of<16>(); }
+int adj_occupancy(int rows, bool reverse) {
+  return rows == 4 ? occupancy_of<4>(reverse) : occupancy_of<16>(reverse);
+}
 
 cudaError_t launch_adj_copy_in(const TileDesc* set_tiles, const AdjTile* tiles, uint32_t count,
                                uint32_t max_blocks, cudaStream_t s) {
@@ -935,12 +941,15 @@ int Adjoint::create(TileSet* set, uint32_t ticks, uint32_t every, const uint32_t
     set_err(err, std::string("water_live: sweep setup: ") + cudaGetErrorString(e));
     return WL_ERR_CUDA;
   }
-  const int occ = adj_occupancy(rows_);
-  if (occ <= 0 || dev_sms <= 0) {
+  // The forward marches and the reverse march each get the grid their own residency allows.
+  const int occ_fwd = adj_occupancy(rows_, false), occ_rev = adj_occupancy(rows_, true);
+  if (occ_fwd <= 0 || occ_rev <= 0 || dev_sms <= 0) {
     set_err(err, "water_live: the adjoint's kernels cannot be resident on this device");
     return WL_ERR_CUDA;
   }
-  grid_ = int(std::min<uint64_t>((n_items_ + kWarps - 1u) / kWarps, uint64_t(dev_sms) * occ));
+  const uint64_t warps_needed = (n_items_ + kWarps - 1u) / kWarps;
+  grid_fwd_ = int(std::min<uint64_t>(warps_needed, uint64_t(dev_sms) * occ_fwd));
+  grid_rev_ = int(std::min<uint64_t>(warps_needed, uint64_t(dev_sms) * occ_rev));
   return check_flags(err);
 }
 
@@ -964,7 +973,7 @@ cudaError_t Adjoint::enqueue(float dt) {
   AdjArgs a{d_tiles_, nt > 1 ? d_item_tile_ : nullptr, d_work_, n_items_, ticks_, every_, 0u, dt};
   for (uint32_t t = 0; t < ticks_; ++t) {
     a.t = t;
-    if ((e = launch_adj_forward(0, rows_, a, grid_, s)) != cudaSuccess) return e;
+    if ((e = launch_adj_forward(0, rows_, a, grid_fwd_, s)) != cudaSuccess) return e;
   }
   if ((e = launch_adj_check(a, nt, s)) != cudaSuccess) return e;
   if ((e = launch_adj_seed(a, nt, s)) != cudaSuccess) return e;
@@ -972,11 +981,11 @@ cudaError_t Adjoint::enqueue(float dt) {
     const uint32_t start = c * every_, end = std::min(start + every_, ticks_);
     for (uint32_t t = start; t + 1u < end; ++t) {
       a.t = t;
-      if ((e = launch_adj_forward(1, rows_, a, grid_, s)) != cudaSuccess) return e;
+      if ((e = launch_adj_forward(1, rows_, a, grid_fwd_, s)) != cudaSuccess) return e;
     }
     for (uint32_t t = end; t-- > start;) {
       a.t = t;
-      if ((e = launch_adj_reverse(rows_, a, grid_, s)) != cudaSuccess) return e;
+      if ((e = launch_adj_reverse(rows_, a, grid_rev_, s)) != cudaSuccess) return e;
     }
   }
   return cudaSuccess;

@@ -62,7 +62,8 @@ struct AdjArgs {
 };
 
 // A work item is 32 columns by 4 or 16 rows (the sweep chooses by the device's SM count).
-int adj_occupancy(int rows);
+// The resident CTAs an SM of the forward marches or (reverse) of the reverse march.
+int adj_occupancy(int rows, bool reverse);
 // The set's current states into checkpoint 0 (grid: max_blocks by count).
 cudaError_t launch_adj_copy_in(const TileDesc* set_tiles, const AdjTile* tiles, uint32_t count,
                                uint32_t max_blocks, cudaStream_t s);
@@ -113,7 +114,7 @@ class Adjoint {
   uint32_t* d_item_tile_ = nullptr;
   WorkCtl* d_work_ = nullptr;
   uint32_t n_items_ = 0;
-  int grid_ = 0;
+  int grid_fwd_ = 0, grid_rev_ = 0;
   int rows_ = 16;
   // zeroed at the start of every sweep: the gradients, speeds, counts and losses
   void* zero_ = nullptr;
