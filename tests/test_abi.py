@@ -173,3 +173,17 @@ def test_an_adjoint_never_created_refuses_every_read(wl_lib):
     assert wl_lib.wl_adjoint_launches(None) == 0
     assert wl_lib.wl_adjoint_device_bytes(None) == 0
     wl_lib.wl_adjoint_destroy(None)
+
+
+def test_a_batch_with_an_empty_or_oversized_tile_is_refused(wl_lib):
+    # Before any device is touched: an empty tile, or one of more than 2^30 cells.
+    cfg = _abi.Config(0, 0, 1.0, 9.81, 0.45, 1e-9, 0, 0, 0, 0, 0)
+    out = C.c_void_p()
+    err = C.create_string_buffer(128)
+    tiles = (_abi.Tile * 2)(_abi.Tile(64, 64, 0, 0, 0, 0), _abi.Tile(0, 8, 0, 0, 0, 0))
+    assert wl_lib.wl_batch_create(C.byref(cfg), None, tiles, 2, C.byref(out), err, 128) == 2
+    assert b"empty grid" in err.value and not out.value
+    tiles[1] = _abi.Tile(40000, 40000, 0, 0, 0, 0)
+    assert wl_lib.wl_batch_create(C.byref(cfg), None, tiles, 2, C.byref(out), err, 128) == 2
+    assert b"2^30" in err.value and not out.value
+    assert wl_lib.wl_batch_create(C.byref(cfg), None, tiles, 0, C.byref(out), err, 128) == 2
