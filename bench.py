@@ -21,7 +21,8 @@ against the reference's CPU step restated in oracle/.
 
 `--impl reference` times the reference's CPU tick (the FP64 solver, water_state::Solver::step,
 restated in oracle/ and checked byte for byte against the reference's own build) on this host's
-cores, on the same workload, a bounded number of ticks a step.
+cores, on the same workload: the same ticks a step from the same initial state. Its process loads
+the oracle's library only (the terrain comes from the numpy generator).
 """
 from __future__ import annotations
 
@@ -160,15 +161,18 @@ def run_reference(args, tile, rank, world):
     s.set_state(tile.h, tile.hu, tile.hv)
     s.set_inputs(tile.bed, None, tile.source)
     max_dt = tile.meta.get("max_dt", 0.01)
-    ticks_per_step = 2
+    # The same ticks a step as the GPU arm, from the same initial state every step.
+    ticks_per_step = tile.meta["ticks"]
     for _ in range(args.warmup):
         for _ in range(ticks_per_step):
             s.step(max_dt)
-    t0 = time.perf_counter()
+    dt = 0.0
     for _ in range(args.steps):
+        s.set_state(tile.h, tile.hu, tile.hv)  # untimed, like the GPU arm's restore
+        t0 = time.perf_counter()
         for _ in range(ticks_per_step):
             s.step(max_dt)
-    dt = time.perf_counter() - t0
+        dt += time.perf_counter() - t0
     value = tile.cells * ticks_per_step * args.steps / dt
     sample = (f"{ticks_per_step} ticks a step of the {tile.nx}x{tile.ny} tile, FP64 reference "
               f"CPU tick (oracle/ restatement, byte-equal to the reference's build), {threads} "
@@ -302,8 +306,8 @@ def run_plain(args, tile, rank, world):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": tile.meta.get("data", "synthetic"),
-        "config": dict(workload_config(tile, ticks, world),
-                       ledger_steps_last_run=ledger["steps"] if ledger else None),
+        "config": workload_config(tile, ticks, world),
+        "ledger_steps_last_run": ledger["steps"] if ledger else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes_per_launch": algo_bytes,
@@ -688,10 +692,13 @@ def main():
                 out = fn(args.steps, args.warmup, args.ticks)
             print(json.dumps(out), flush=True)
         return
+    # The reference arm builds its terrain with the numpy generator (the same doubles), so that
+    # nothing of this library is loaded into its process.
+    terrain = workloads.fbm_numpy if args.impl == "reference" else workloads.fbm
     if args.workload == "plain_2048":
-        tile = workloads.plain_2048()
+        tile = workloads.plain_2048(terrain=terrain)
     elif args.workload == "plain_256":
-        tile = workloads.plain_256()
+        tile = workloads.plain_256(terrain=terrain)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     if args.ticks > 0:

@@ -38,7 +38,7 @@ struct StaticScratch {
 static __device__ __align__(256) StaticScratch g_scratch;
 
 // The descriptor in, the control block emptied (the ledger with no time left to count down, as
-// write_state leaves it), the work counter at zero.
+// write_state leaves it), every word of the work counter at zero.
 __global__ void static_init_kernel(StaticScratch* s, TileDesc d) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   s->desc = d;
@@ -48,6 +48,8 @@ __global__ void static_init_kernel(StaticScratch* s, TileDesc d) {
   s->ctl = c;
   s->work.next = 0u;
   s->work.exited = 0u;
+  s->work.tail = 0u;
+  s->work.pad = 0u;
 }
 
 std::mutex g_mu;

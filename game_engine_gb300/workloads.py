@@ -3,7 +3,9 @@
 Terrain is fBm: six octaves of value noise on an integer-hash lattice (the reference's `mix`,
 water_live_device_tests.cpp:50-56, so the lattice is the same on every host), lacunarity 2, gain
 0.5, base period side / 4, smoothstep-weighted bilinear interpolation in double, normalised to
-[0, H]. Every configuration has a fixed 64-bit seed.
+[0, H]. Every configuration has a fixed 64-bit seed. Each workload takes its terrain generator as
+`terrain`: the library's threaded `fbm` by default, or `fbm_numpy`, which gives the same doubles
+without loading the library (the reference CPU arm and the fixture generators use it).
 
   plain_256   256 x 256, H 20 m, dry but for a centred 32 x 32 column of 2 m; 1000 ticks.
   plain_2048  2048 x 2048, H 50 m, depth U[0, 0.5] m, rain 1e-5 m a tick; 500 ticks.
@@ -140,17 +142,17 @@ def column(nx, ny, x0, y0, side=32, depth=2.0):
     return h.ravel()
 
 
-def plain_256() -> Tile:
+def plain_256(terrain=fbm) -> Tile:
     n = 256
-    bed = fbm(n, n, 20.0, SEEDS["plain_256"])
+    bed = terrain(n, n, 20.0, SEEDS["plain_256"])
     h = column(n, n, n // 2 - 16, n // 2 - 16)
     return Tile(n, n, bed, h, meta=dict(ticks=1000, max_dt=MAX_DT, name="plain_256",
                                         data="synthetic: seeded 6-octave fBm terrain 0-20 m, "
                                              "dry but a centred 32 x 32 column of 2 m"))
 
 
-def plain_2048(side: int = 2048) -> Tile:
-    bed = fbm(side, side, 50.0, SEEDS["plain_2048"])
+def plain_2048(side: int = 2048, terrain=fbm) -> Tile:
+    bed = terrain(side, side, 50.0, SEEDS["plain_2048"])
     rng = np.random.Generator(np.random.PCG64(SEEDS["plain_2048"] & 0xFFFFFFFF))
     h = rng.uniform(0.0, 0.5, side * side)
     rain = np.full(side * side, 1e-5 / MAX_DT)  # 1e-5 m a tick at dt = max_dt
@@ -183,14 +185,15 @@ def tile_sides(count: int, seed: int, sides=TILE_SIDES):
     return [int(sides[k]) for k in rng.integers(0, len(sides), count)]
 
 
-def tiles_4096(count: int = 4096, sides=None, seed: int | None = None, with_bed: bool = True):
+def tiles_4096(count: int = 4096, sides=None, seed: int | None = None, with_bed: bool = True,
+               terrain=fbm):
     """The batched workload: `count` tiles of seeded sides, each its own fBm and 2 m column."""
     seed = SEEDS["tiles_4096"] if seed is None else seed
     sides = tile_sides(count, seed) if sides is None else sides
     rng = np.random.Generator(np.random.PCG64((seed >> 32) & 0xFFFFFFFF))
     out = []
     for k, s in enumerate(sides):
-        bed = fbm(s, s, 20.0, seed + 7919 * (k + 1)) if with_bed else np.zeros(s * s)
+        bed = terrain(s, s, 20.0, seed + 7919 * (k + 1)) if with_bed else np.zeros(s * s)
         x0 = int(rng.integers(0, s - 32 + 1))
         y0 = int(rng.integers(0, s - 32 + 1))
         out.append(Tile(s, s, bed, column(s, s, x0, y0), meta=dict(index=k)))
@@ -220,9 +223,9 @@ def probe_cells(cells: int, count: int, seed: int) -> np.ndarray:
     return np.sort(out)
 
 
-def adjoint_512(side: int = 512) -> Tile:
+def adjoint_512(side: int = 512, terrain=fbm) -> Tile:
     seed = SEEDS["adjoint_512"]
-    bed = fbm(side, side, ADJOINT_RELIEF_M, seed)
+    bed = terrain(side, side, ADJOINT_RELIEF_M, seed)
     return Tile(side, side, bed, lake(side, side, bed, ADJOINT_LEVEL_M, ADJOINT_RISE_M),
                 source=np.zeros(side * side),
                 meta=dict(ticks=ADJOINT_TICKS, every=ADJOINT_EVERY, max_dt=MAX_DT,
@@ -233,12 +236,12 @@ def adjoint_512(side: int = 512) -> Tile:
 ADJOINT_TILE_SIDES = (64, 128, 192, 256, 320, 384, 448, 512)
 
 
-def tiles_256_adjoint(count: int = 256) -> list:
+def tiles_256_adjoint(count: int = 256, terrain=fbm) -> list:
     seed = SEEDS["tiles_256_adjoint"]
     sides = tile_sides(count, seed, ADJOINT_TILE_SIDES)
     out = []
     for k, s in enumerate(sides):
-        bed = fbm(s, s, ADJOINT_RELIEF_M, seed + 7919 * (k + 1))
+        bed = terrain(s, s, ADJOINT_RELIEF_M, seed + 7919 * (k + 1))
         out.append(Tile(s, s, bed, lake(s, s, bed, ADJOINT_LEVEL_M, ADJOINT_RISE_M, phase=0.1 * k),
                         source=np.zeros(s * s),
                         meta=dict(index=k, probes=probe_cells(s * s, PROBES, seed + k))))

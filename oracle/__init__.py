@@ -31,11 +31,27 @@ def build(quiet: bool = True) -> None:
                    stdout=subprocess.DEVNULL if quiet else None)
 
 
-def build_ref(reference_root: str = "/root/reference") -> bool:
-    """Compiles the reference's own solver when its sources are present; True if built."""
-    subprocess.run([os.path.join(HERE, "build_ref.sh"), reference_root], check=True,
-                   stdout=subprocess.DEVNULL)
+def build_ref(reference_root: str | None = None) -> bool:
+    """Compiles the reference's own solver when its sources are present; True if built. The root
+    is `reference_root`, else $WL_REFERENCE_ROOT, else the recipe's own (oracle/build_ref.sh)."""
+    cmd = [os.path.join(HERE, "build_ref.sh")]
+    if reference_root:
+        cmd.append(reference_root)
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
     return os.path.exists(REF_PATH)
+
+
+def reference_root() -> str | None:
+    """The reference's source root: $WL_REFERENCE_ROOT, else the root oracle/_ref was built from
+    (recorded by oracle/build_ref.sh); None when neither names a directory that exists."""
+    root = os.environ.get("WL_REFERENCE_ROOT")
+    if not root:
+        try:
+            with open(os.path.join(HERE, "_ref", "reference_root")) as f:
+                root = f.read().strip()
+        except OSError:
+            return None
+    return root if root and os.path.isdir(root) else None
 
 
 def lib():

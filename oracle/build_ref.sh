@@ -5,12 +5,16 @@
 # oracle/_ref/libwsref.so behind oracle/ref_shim.cpp. Nothing is copied out of the reference; the
 # reference's own build system (CMake, FetchContent) is not run.
 #
-#   oracle/build_ref.sh [REFERENCE_ROOT]     (default: /root/reference)
+#   oracle/build_ref.sh [REFERENCE_ROOT]
 #
-# Exits 0 without building when the reference's sources are absent (the GPU host has none).
+# The root is the argument, else $WL_REFERENCE_ROOT, else the place this recipe reads the
+# reference's sources from on the build machine (below). The root it built from is recorded in
+# oracle/_ref/reference_root, so that the tests and fixture generators that read the reference's
+# headers find them without naming a path. Exits 0 without building when the reference's sources
+# are absent (a machine that only runs the tests has none).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${WL_REFERENCE_ROOT:-/root/reference}}"
 OUT="$HERE/_ref"
 if [[ ! -f "$REF/domain/water_state/src/water_state.cpp" ]]; then
   echo "build_ref: no reference sources at $REF; skipped"
@@ -43,4 +47,5 @@ done
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -shared -o "$OUT/libwsref.so" "${OBJ[@]}" -lpthread
 rm -f "${OBJ[@]}"
+printf '%s\n' "$REF" > "$OUT/reference_root"
 echo "build_ref: $OUT/libwsref.so"
