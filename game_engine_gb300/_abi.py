@@ -76,13 +76,15 @@ class Landed(C.Structure):
     """wl_landed: a landed tick's read-back record."""
     _fields_ = [("tick", C.c_uint32), ("substeps", C.c_uint32), ("shortest_s", C.c_float),
                 ("longest_s", C.c_float), ("time_hi", C.c_float), ("time_lo", C.c_float),
-                ("steps", C.c_uint32), ("events", C.c_uint32)]
+                ("steps", C.c_uint32), ("events", C.c_uint32), ("dropped", C.c_uint32),
+                ("dropped_total", C.c_uint32), ("lag", C.c_uint32), ("frozen", C.c_uint32)]
 
 
 class QueueStatus(C.Structure):
     """wl_queue_status: the queue's counts."""
     _fields_ = [("pushed", C.c_uint32), ("begun", C.c_uint32), ("landed", C.c_uint32),
-                ("active", C.c_uint32), ("substeps", C.c_uint32), ("pad", C.c_uint32 * 3)]
+                ("active", C.c_uint32), ("substeps", C.c_uint32), ("dropped", C.c_uint32),
+                ("frozen", C.c_uint32), ("freezes", C.c_uint32)]
 
 
 class WsCarriedConfig(C.Structure):
@@ -128,6 +130,9 @@ SIGNATURES = {
     "wl_read_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
     "wl_read_state_bits": (C.c_int, [C.c_void_p, _fp, C.c_size_t, *_err]),
     "wl_read_ledger": (C.c_int, [C.c_void_p, C.POINTER(Ledger), *_err]),
+    "wl_settled": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, C.c_float, C.c_float,
+                             C.POINTER(C.c_uint8), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                             *_err]),
     "wl_set_bed": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_double, *_err]),
     "wl_set_manning": (C.c_int, [C.c_void_p, _dp, C.c_size_t, *_err]),
     "wl_set_source": (C.c_int, [C.c_void_p, _dp, C.c_size_t, C.c_uint32, C.c_int, *_err]),
@@ -148,6 +153,9 @@ SIGNATURES = {
     "wl_batch_tile_count": (C.c_uint32, [C.c_void_p]),
     "wl_batch_cell_count": (C.c_uint64, [C.c_void_p]),
     "wl_batch_tile_first": (C.c_uint64, [C.c_void_p, C.c_uint32]),
+    "wl_batch_settled": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, C.c_float, C.c_float,
+                                   C.POINTER(C.c_uint8), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float), C.c_uint32, *_err]),
     "wl_batch_write_tile_state": (C.c_int, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, C.c_size_t,
                                             *_err]),
     "wl_batch_write_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
@@ -194,6 +202,7 @@ SIGNATURES = {
     "wl_queue_push": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.POINTER(Event), C.c_uint32,
                                 _fp, C.c_size_t, *_err]),
     "wl_queue_enqueue_slots": (C.c_int, [C.c_void_p, wl_stream, C.c_uint32]),
+    "wl_queue_set_limits": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, *_err]),
     "wl_queue_run_slots": (C.c_int, [C.c_void_p, C.c_uint32, *_err]),
     "wl_queue_status_read": (C.c_int, [C.c_void_p, C.POINTER(QueueStatus), *_err]),
     "wl_queue_read_landed": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(Landed),

@@ -99,6 +99,22 @@ class Batch:
                                                     hv.ctypes.data_as(_dp), h.size, self._buf,
                                                     len(self._buf)))
 
+    def settled(self, h, hu, hv, depth_bound_m, momentum_bound_m2_s):
+        """The settled check of every tile against a steady state (whole-batch arrays, tile after
+        tile): (settled bools, depth deviations, momentum deviations), one each a tile."""
+        h, hu, hv = self._arr(h), self._arr(hu), self._arr(hv)
+        n = self.tile_count
+        ok8 = np.zeros(n, dtype=np.uint8)
+        dd = np.zeros(n, dtype=np.float32)
+        dq = np.zeros(n, dtype=np.float32)
+        self._check(lib().wl_batch_settled(self._h, h.ctypes.data_as(_dp), hu.ctypes.data_as(_dp),
+                                           hv.ctypes.data_as(_dp), self.cells,
+                                           float(depth_bound_m), float(momentum_bound_m2_s),
+                                           ok8.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                           dd.ctypes.data_as(_fp), dq.ctypes.data_as(_fp), n,
+                                           self._buf, len(self._buf)))
+        return ok8.astype(bool), dd, dq
+
     def set_bed(self, bed, datum=0.0):
         b = self._arr(bed)
         self._check(lib().wl_batch_set_bed(self._h, b.ctypes.data_as(_dp), self.cells,

@@ -204,6 +204,19 @@ int wl_read_ledger(wl_step* s, wl_ledger* out, char* err, size_t err_len) {
   return WL_OK;
 }
 
+int wl_settled(wl_step* s, const double* h, const double* hu, const double* hv, size_t n,
+               float depth_bound, float momentum_bound, uint8_t* settled, float* depth_dev,
+               float* momentum_dev, char* err, size_t err_len) {
+  if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (n != s->cells || h == nullptr || hu == nullptr || hv == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: a steady state that does not fit the grid");
+  std::string msg;
+  if (!s->set.settled(false, 0, h, hu, hv, depth_bound, momentum_bound, settled, depth_dev,
+                      momentum_dev, &msg))
+    return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
 int wl_set_bed(wl_step* s, const double* bed, size_t n, double datum, char* err, size_t err_len) {
   if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
   if (n != s->cells || bed == nullptr)
@@ -493,6 +506,18 @@ int wl_queue_status_read(wl_queue* queue, wl_queue_status* out, char* err, size_
   out->landed = c.landed;
   out->active = c.active;
   out->substeps = c.substeps;
+  out->dropped = c.dropped;
+  out->frozen = c.frozen;
+  out->freezes = c.freezes;
+  return WL_OK;
+}
+
+int wl_queue_set_limits(wl_queue* queue, uint32_t lag_limit_ticks, uint32_t max_slots, char* err,
+                        size_t err_len) {
+  if (queue == nullptr || queue->owner == nullptr || !queue->q.valid())
+    return fail(err, err_len, WL_ERR_INVALID, "water_live: no queue");
+  std::string msg;
+  if (!queue->q.set_limits(lag_limit_ticks, max_slots, &msg)) return cuda_fail(err, err_len, msg);
   return WL_OK;
 }
 

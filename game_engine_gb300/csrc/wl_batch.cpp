@@ -255,6 +255,22 @@ int wl_batch_write_tile_state(wl_batch* b, uint32_t tile, const double* h, const
   return WL_OK;
 }
 
+int wl_batch_settled(wl_batch* b, const double* h, const double* hu, const double* hv,
+                     size_t total, float depth_bound, float momentum_bound, uint8_t* settled,
+                     float* depth_dev, float* momentum_dev, uint32_t count, char* err,
+                     size_t err_len) {
+  if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
+  if (total != b->set.total_cells() || h == nullptr || hu == nullptr || hv == nullptr)
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: steady states that do not fit the tiles");
+  if (count != b->set.tile_count())
+    return fail(err, err_len, WL_ERR_SIZE, "water_live: outputs that do not fit the tiles");
+  std::string msg;
+  if (!b->set.settled(true, 0, h, hu, hv, depth_bound, momentum_bound, settled, depth_dev,
+                      momentum_dev, &msg))
+    return cuda_fail(err, err_len, msg);
+  return WL_OK;
+}
+
 int wl_batch_set_bed(wl_batch* b, const double* bed, size_t total, double datum, char* err,
                      size_t err_len) {
   if (!valid(b)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);

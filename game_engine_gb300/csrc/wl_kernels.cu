@@ -38,6 +38,8 @@
 #include "wl_device.cuh"
 #include "wl_kernels.h"
 
+#include <algorithm>
+
 namespace wlc {
 
 namespace {
@@ -1325,6 +1327,43 @@ __global__ void copy_state_kernel(const TileDesc* tiles, uint32_t tile, float* d
     dst[i] = p[i];
 }
 
+// ---- the settled check (ADR-0080 decision 4) ---------------------------------------------------
+
+// Per tile, the largest |h - h*| and the largest of |hu - hu*| and |hv - hv*| over its cells, the
+// steady state h*, hu*, hv* given as doubles and rounded to f32 as the step rounds its state.
+// blockIdx.y is the tile (tile0 + y), blockIdx.x a stride over its cells; the tile's cells start at
+// first[t] in the arrays (0 where `first` is null). The maxima go into dev[2 y], dev[2 y + 1] by
+// atomicMax on the bits of non-negative floats: exact in any order, and a NaN's bits exceed every
+// number's, so a tile holding a NaN never settles.
+__global__ void __launch_bounds__(256) settled_kernel(const TileDesc* tiles, uint32_t tile0,
+                                                      const uint64_t* first, const double* h,
+                                                      const double* hu, const double* hv,
+                                                      uint32_t* dev) {
+  const uint32_t t = tile0 + blockIdx.y;
+  const TileDesc& T = tiles[t];
+  const size_t n = size_t(T.nx) * T.ny;
+  const size_t base = first == nullptr ? 0 : size_t(first[t]);
+  const float* st = T.state[T.ctl->cur];
+  uint32_t dd = 0u, dq = 0u;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const float a = fabsf(__fsub_rn(st[i], __double2float_rn(h[base + i])));
+    const float b = fabsf(__fsub_rn(st[n + i], __double2float_rn(hu[base + i])));
+    const float c = fabsf(__fsub_rn(st[2 * n + i], __double2float_rn(hv[base + i])));
+    dd = max(dd, __float_as_uint(a));
+    dq = max(dq, max(__float_as_uint(b), __float_as_uint(c)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dd = max(dd, __shfl_xor_sync(0xffffffffu, dd, o));
+    dq = max(dq, __shfl_xor_sync(0xffffffffu, dq, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&dev[2 * blockIdx.y], dd);
+    atomicMax(&dev[2 * blockIdx.y + 1], dq);
+  }
+}
+
 // ---- whole batches: arrays of every tile's cells, tile after tile ------------------------------
 
 // The tile holding global cell index k of the batch (first[t] = the tile's first cell).
@@ -1478,6 +1517,21 @@ int grid_for(size_t n) {
 }  // namespace
 
 // ---- host-side launchers (wl_kernels.h) ---------------------------------------------------------
+
+cudaError_t launch_settled(const TileDesc* tiles, uint32_t tile0, uint32_t count,
+                           const uint64_t* first, uint64_t largest, const double* h,
+                           const double* hu, const double* hv, uint32_t* dev, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  if (cudaMemsetAsync(dev, 0, size_t(count) * 2 * sizeof(uint32_t), s) != cudaSuccess)
+    return cudaGetLastError();
+  const uint64_t chunks = std::min<uint64_t>((largest + 4095) / 4096, 1024);
+  for (uint32_t k = 0; k < count; k += 65535u) {
+    const uint32_t c = std::min<uint32_t>(65535u, count - k);
+    settled_kernel<<<dim3(unsigned(std::max<uint64_t>(chunks, 1)), c), 256, 0, s>>>(
+        tiles, tile0 + k, first, h, hu, hv, dev + 2 * size_t(k));
+  }
+  return cudaGetLastError();
+}
 
 size_t tick_smem_bytes(BlockShape shape) {
   switch (shape) {

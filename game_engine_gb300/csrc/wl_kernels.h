@@ -73,6 +73,13 @@ cudaError_t launch_scatter_plane(TileDesc* tiles, uint32_t count, const uint64_t
 // Every tile's current copy, four planes a tile (4 * first[t] floats before tile t).
 cudaError_t launch_gather_state(const TileDesc* tiles, uint32_t count, const uint64_t* first,
                                 uint64_t total, float* dst, cudaStream_t s);
+// The settled check of tiles tile0 .. tile0 + count - 1 against a steady state (device doubles,
+// tile t's cells from first[t], or from 0 where `first` is null): dev[2 k] and dev[2 k + 1] get
+// the bits of tile tile0 + k's largest depth and momentum deviations. `largest`: the most cells a
+// tile holds.
+cudaError_t launch_settled(const TileDesc* tiles, uint32_t tile0, uint32_t count,
+                           const uint64_t* first, uint64_t largest, const double* h,
+                           const double* hu, const double* hv, uint32_t* dev, cudaStream_t s);
 // A flush (dt_main with max_dt 0) of every tile.
 cudaError_t launch_flush_all(bool fixed, const TileDesc* tiles, uint32_t count, cudaStream_t s);
 

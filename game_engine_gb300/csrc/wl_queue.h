@@ -49,6 +49,13 @@ struct QueueCtl {
   uint64_t values_end;    // its values' end
   uint64_t events_done;   // events whose values the device no longer reads
   uint64_t values_done;   // arena values the device no longer reads
+  // The lag control (water_live.md:90-92; wl_queue_set_limits).
+  uint32_t lag_limit;  // ticks pushed and not landed past which a begin freezes the domain (0: off)
+  uint32_t frozen;     // the domain is frozen: each begun tick is dropped
+  uint32_t dropping;   // the tick in flight is a dropped one
+  uint32_t dropped;    // ticks dropped
+  uint32_t freezes;    // times the domain froze
+  uint32_t lag;        // the lag when the tick in flight began
 };
 
 class TickQueue {
@@ -62,7 +69,9 @@ class TickQueue {
   // WL_OK, or WL_ERR_REFUSED (no room yet), WL_ERR_ARGUMENT, WL_ERR_CUDA with `err` set.
   int push(uint32_t tick, float length_s, const wl_event* events, uint32_t n_events,
            const float* values, size_t n_values, std::string* err);
+  // At most max_slots slots a call when max_slots > 0 (wl_queue_set_limits).
   cudaError_t enqueue(cudaStream_t s, uint32_t slots);
+  bool set_limits(uint32_t lag_limit, uint32_t max_slots, std::string* err);
   bool read_ctl(QueueCtl& out, std::string* err);
   bool read_landed(uint32_t first, uint32_t count, wl_landed* out, std::string* err);
   uint64_t device_bytes() const { return bytes_; }
@@ -82,6 +91,7 @@ class TickQueue {
   uint32_t* d_seen_ = nullptr;  // each tile's step count at the last settle
   uint32_t tiles_ = 0;
   uint32_t records_ = 0, max_events_ = 0, arena_ = 0;
+  uint32_t max_slots_ = 0;  // 0: no ceiling
   uint32_t pushed_ = 0;        // records pushed
   uint64_t events_pushed_ = 0;  // events pushed
   uint64_t values_pushed_ = 0;  // arena values pushed (with the padding that keeps a push whole)

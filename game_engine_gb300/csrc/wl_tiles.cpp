@@ -566,6 +566,44 @@ bool TileSet::write_all(const double* h, const double* hu, const double* hv, std
   return wait(err);
 }
 
+bool TileSet::settled(bool all, uint32_t tile, const double* h, const double* hu,
+                      const double* hv, float depth_bound, float momentum_bound, uint8_t* out,
+                      float* depth_dev, float* momentum_dev, std::string* err) {
+  if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
+  const uint32_t count = all ? tile_count() : 1u;
+  const size_t n = all ? total_cells_ : cells(tile);
+  uint64_t largest = 0;
+  for (uint32_t k = 0; k < count; ++k) largest = std::max<uint64_t>(largest, cells(all ? k : tile));
+  const size_t values = align_up(3 * n * sizeof(double));
+  if (!ensure_staging(values + size_t(count) * 2 * sizeof(uint32_t), err)) return false;
+  double* d = static_cast<double*>(staging_);
+  uint32_t* dev = reinterpret_cast<uint32_t*>(static_cast<char*>(staging_) + values);
+  std::vector<uint32_t> bits(size_t(count) * 2);
+  if (!check(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of the steady depth") ||
+      !check(cudaMemcpyAsync(d + n, hu, n * sizeof(double), cudaMemcpyHostToDevice, stream_), err,
+             "upload of the steady momentum") ||
+      !check(cudaMemcpyAsync(d + 2 * n, hv, n * sizeof(double), cudaMemcpyHostToDevice, stream_),
+             err, "upload of the steady momentum") ||
+      !check(launch_settled(d_desc_, all ? 0u : tile, count, all ? d_first_ : nullptr, largest, d,
+                            d + n, d + 2 * n, dev, stream_),
+             err, "the settled check") ||
+      !check(cudaMemcpyAsync(bits.data(), dev, bits.size() * sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, stream_),
+             err, "read-back of the settled check") ||
+      !wait(err))
+    return false;
+  for (uint32_t k = 0; k < count; ++k) {
+    float dd, dq;
+    std::memcpy(&dd, &bits[2 * k], 4);
+    std::memcpy(&dq, &bits[2 * k + 1], 4);
+    if (depth_dev != nullptr) depth_dev[k] = dd;
+    if (momentum_dev != nullptr) momentum_dev[k] = dq;
+    if (out != nullptr) out[k] = (dd <= depth_bound && dq <= momentum_bound) ? 1u : 0u;
+  }
+  return true;
+}
+
 bool TileSet::set_plane_all(int which, const double* v, double datum, std::string* err) {
   if (!check(cudaSetDevice(device_), err, "cudaSetDevice")) return false;
   const size_t n = total_cells_;

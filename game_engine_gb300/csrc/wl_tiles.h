@@ -76,6 +76,12 @@ class TileSet {
   bool read_all_bits(float* out, std::string* err);
   bool flush_all(std::string* err);
   bool read_all_ctl(TileCtl* out, std::string* err);
+  // The settled check against a steady state (doubles): of every tile, the arrays tile after tile
+  // (`all`), or of tile `tile` alone, its own nx * ny cells. Per tile, the largest depth and
+  // momentum deviations (f32), and settled = both within their bounds. Outputs may be null.
+  bool settled(bool all, uint32_t tile, const double* h, const double* hu, const double* hv,
+               float depth_bound, float momentum_bound, uint8_t* settled, float* depth_dev,
+               float* momentum_dev, std::string* err);
   uint64_t first_cell(uint32_t tile) const { return first_[tile]; }
   // A copy of everything a tick changes (states, records, control blocks), and its restoration:
   // the autotuner's trial ticks leave the simulation where it was.

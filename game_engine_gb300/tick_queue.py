@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _abi, lib
 
-EVENT_BED, EVENT_SOURCE, EVENT_MANNING = 0, 1, 2
+EVENT_BED, EVENT_SOURCE, EVENT_MANNING, EVENT_STATE = 0, 1, 2, 3
 ERR_REFUSED = 5
 MAX_RECORDS = 64
 
@@ -24,11 +24,12 @@ _fp = C.POINTER(C.c_float)
 @dataclass
 class Event:
     """A rectangle of one plane (EVENT_*) of one tile replaced by ``values`` (h rows of w, row by
-    row); tile 0 for a step's queue."""
+    row); tile 0 for a step's queue. An EVENT_STATE's values are (3, h, w): depth, then the two
+    momenta (a waking tile's starting state)."""
     kind: int
     x0: int
     y0: int
-    values: np.ndarray  # shape (h, w)
+    values: np.ndarray  # shape (h, w), or (3, h, w) for EVENT_STATE
     tile: int = 0
 
 
@@ -76,7 +77,7 @@ class TickQueue:
         vals = []
         for k, e in enumerate(events):
             v = np.ascontiguousarray(e.values, dtype=np.float32)
-            h, w = v.shape
+            h, w = v.shape[-2:]
             evs[k] = _abi.Event(int(e.kind), int(e.x0), int(e.y0), int(w), int(h), int(e.tile))
             vals.append(v.ravel())
         flat = np.concatenate(vals) if vals else np.zeros(1, np.float32)
@@ -94,6 +95,13 @@ class TickQueue:
             return False
         return True
 
+    def set_limits(self, lag_limit_ticks: int = 0, max_slots: int = 0) -> bool:
+        """The lag control (water_live.md:90-92): past ``lag_limit_ticks`` ticks pushed and not
+        landed the domain freezes and drops ticks until the queue drains; ``max_slots`` caps the
+        slots one call enqueues. 0 turns either off."""
+        return self._ok(lib().wl_queue_set_limits(self._h, int(lag_limit_ticks), int(max_slots),
+                                                  self._buf, len(self._buf)))
+
     def run_slots(self, slots: int) -> bool:
         return self._ok(lib().wl_queue_run_slots(self._h, int(slots), self._buf, len(self._buf)))
 
@@ -103,7 +111,7 @@ class TickQueue:
                                                    len(self._buf))):
             return None
         return dict(pushed=s.pushed, begun=s.begun, landed=s.landed, active=s.active,
-                    substeps=s.substeps)
+                    substeps=s.substeps, dropped=s.dropped, frozen=s.frozen, freezes=s.freezes)
 
     def landed(self, first: int, count: int):
         """The read-back records of landings first .. first + count - 1, as dicts."""
@@ -113,7 +121,8 @@ class TickQueue:
             return None
         return [dict(tick=r.tick, substeps=r.substeps, shortest_s=r.shortest_s,
                      longest_s=r.longest_s, time_hi=r.time_hi, time_lo=r.time_lo, steps=r.steps,
-                     events=r.events) for r in out[:count]]
+                     events=r.events, dropped=r.dropped, dropped_total=r.dropped_total,
+                     lag=r.lag, frozen=r.frozen) for r in out[:count]]
 
     @staticmethod
     def launches_per_slot() -> int:

@@ -164,6 +164,19 @@ class DeviceStep:
                     roundoff_m3=out.roundoff_m3, time_s=out.time_s, remaining_s=out.remaining_s,
                     steps=int(out.steps))
 
+    def settled(self, h, hu, hv, depth_bound_m: float, momentum_bound_m2_s: float):
+        """The settled check against a steady state (ADR-0080 decision 4): (settled, largest depth
+        deviation, largest momentum deviation), or None on an error."""
+        h, hu, hv = _f64(h), _f64(hu), _f64(hv)
+        ok8 = C.c_uint8(0)
+        dd, dq = C.c_float(0.0), C.c_float(0.0)
+        if not self._ok(lib().wl_settled(self._h, h.ctypes.data_as(_dp), hu.ctypes.data_as(_dp),
+                                         hv.ctypes.data_as(_dp), h.size, float(depth_bound_m),
+                                         float(momentum_bound_m2_s), C.byref(ok8), C.byref(dd),
+                                         C.byref(dq), self._buf, len(self._buf))):
+            return None
+        return bool(ok8.value), float(dd.value), float(dq.value)
+
     def set_bed(self, bed_m, datum_m: float = 0.0) -> bool:
         b = _f64(bed_m)
         return self._ok(lib().wl_set_bed(self._h, b.ctypes.data_as(_dp), b.size, float(datum_m),

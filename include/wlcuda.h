@@ -134,6 +134,13 @@ int wl_read_state(wl_step* step, double* depth, double* momentum_x, double* mome
 int wl_read_state_bits(wl_step* step, float* planes, size_t count, char* err, size_t err_len);
 /* DeviceStep::read_ledger (water_live.cpp:349-381): a flush, then the pairs widened. */
 int wl_read_ledger(wl_step* step, wl_ledger* out, char* err, size_t err_len);
+/* The settled check of wl_batch_settled on a step (n = its cells): its largest depth and momentum
+ * deviations from the steady state h*, hu*, hv*, and settled = both within the bounds. No
+ * counterpart in DeviceStep (the reference designs the check, ADR-0080 decision 4, W176). */
+int wl_settled(wl_step* step, const double* depth, const double* momentum_x,
+               const double* momentum_y, size_t n, float depth_bound_m, float momentum_bound_m2_s,
+               uint8_t* settled, float* depth_dev_m, float* momentum_dev_m2_s, char* err,
+               size_t err_len);
 
 /* DeviceStep::set_bed (water_live.cpp:439-447): bed_m - datum_m in double, rounded once. */
 int wl_set_bed(wl_step* step, const double* bed_m, size_t n, double datum_m, char* err,
@@ -228,6 +235,18 @@ int wl_batch_write_state(wl_batch* batch, const double* depth, const double* mom
 int wl_batch_write_tile_state(wl_batch* batch, uint32_t tile, const double* depth,
                               const double* momentum_x, const double* momentum_y, size_t n,
                               char* err, size_t err_len);
+/* The settled check of ADR-0080 decision 4 (a tile starts from the baked answer and retires to it
+ * when its state has settled back within a stated bound; the retiring write is
+ * wl_batch_write_tile_state): per tile, the largest |h - h*| over its cells and the largest of
+ * |hu - hu*| and |hv - hv*|, against a steady state h*, hu*, hv* given as doubles tile after tile
+ * (total = all cells, as wl_batch_write_state's arrays) and rounded to f32 as the step rounds its
+ * own state; settled[t] = 1 when both are within depth_bound_m and momentum_bound_m2_s. The maxima
+ * are order-free: the same bytes every run. Each output (count = the tiles) may be null. The
+ * reference designs the check (W176) and has not built it. Waits for the device. */
+int wl_batch_settled(wl_batch* batch, const double* depth, const double* momentum_x,
+                     const double* momentum_y, size_t total, float depth_bound_m,
+                     float momentum_bound_m2_s, uint8_t* settled, float* depth_dev_m,
+                     float* momentum_dev_m2_s, uint32_t count, char* err, size_t err_len);
 int wl_batch_set_bed(wl_batch* batch, const double* bed_m, size_t total, double datum_m, char* err,
                      size_t err_len);
 int wl_batch_set_manning(wl_batch* batch, const double* manning, size_t total, char* err,
@@ -349,13 +368,20 @@ int wl_tick_noalloc(const wl_config* config, int fixed_ops, const float* planes_
 typedef struct wl_queue wl_queue;
 
 enum {
-  WL_EVENT_BED = 0,    /* the bed's heights over the rectangle (metres, the step's f32 datum) */
-  WL_EVENT_SOURCE = 1, /* the source over the rectangle (m/s); the step must have a source on */
-  WL_EVENT_MANNING = 2 /* Manning's n over the rectangle; the step must have Manning on */
+  WL_EVENT_BED = 0,     /* the bed's heights over the rectangle (metres, the step's f32 datum) */
+  WL_EVENT_SOURCE = 1,  /* the source over the rectangle (m/s); the step must have a source on */
+  WL_EVENT_MANNING = 2, /* Manning's n over the rectangle; the step must have Manning on */
+  /* The state over the rectangle: 3 * w * h values, the depths' rectangle, then hu's, then hv's
+   * (the remainder plane there becomes 0). The apply pass that writes a waking tile's starting
+   * state at its tick's boundary (water_live.md:80; ADR-0080 decision 4: a tile starts from the
+   * baked answer). In order: the tile's pending records are folded into its ledger (dt_main with
+   * max_dt 0, the flush), the rectangle is written, and the tile's records become those of its
+   * new state (prime_main, slang:373-386). */
+  WL_EVENT_STATE = 3
 };
 
 /* One event: a rectangle of one plane of one tile replaced by w * h values, row by row (tile 0
- * for a step's queue). */
+ * for a step's queue; 3 * w * h for WL_EVENT_STATE). */
 typedef struct wl_event {
   uint32_t kind;
   uint32_t x0, y0, w, h;
@@ -363,7 +389,10 @@ typedef struct wl_event {
 } wl_event;
 
 /* What a landed tick leaves (water_live.md:94): its number, its sub-steps, its shortest and
- * longest sub-step, and the ledger's time and step count when it landed. */
+ * longest sub-step, and the ledger's time and step count when it landed; whether it was dropped
+ * (stepped by none of its sub-steps, its events applied all the same), the drops so far, the lag
+ * when it began (ticks pushed and not landed, itself included) and whether the domain was frozen
+ * after it landed. */
 typedef struct wl_landed {
   uint32_t tick;
   uint32_t substeps;
@@ -373,15 +402,21 @@ typedef struct wl_landed {
   float time_lo;
   uint32_t steps;
   uint32_t events;
+  uint32_t dropped;
+  uint32_t dropped_total;
+  uint32_t lag;
+  uint32_t frozen;
 } wl_landed;
 
 typedef struct wl_queue_status {
-  uint32_t pushed;  /* ticks pushed since the queue was made */
-  uint32_t begun;   /* ticks begun */
-  uint32_t landed;  /* ticks landed */
-  uint32_t active;  /* 1 while a begun tick has not landed */
+  uint32_t pushed;   /* ticks pushed since the queue was made */
+  uint32_t begun;    /* ticks begun */
+  uint32_t landed;   /* ticks landed (dropped ones included); pushed - landed is the lag */
+  uint32_t active;   /* 1 while a begun tick has not landed */
   uint32_t substeps; /* sub-steps of the tick in flight */
-  uint32_t pad[3];
+  uint32_t dropped;  /* ticks dropped by a freeze */
+  uint32_t frozen;   /* 1 while the domain is frozen */
+  uint32_t freezes;  /* times the domain froze */
 } wl_queue_status;
 
 /* A queue of `records` ticks (at most 64 in flight: water_live.md:84) over a step, with an event
@@ -401,6 +436,17 @@ void wl_queue_destroy(wl_queue* queue);
 int wl_queue_push(wl_queue* queue, uint32_t tick, float length_s, const wl_event* events,
                   uint32_t n_events, const float* values, size_t n_values, char* err,
                   size_t err_len);
+/* The lag control of water_live.md:90-92 (0: off, the default for both):
+ *   - lag_limit_ticks: when a slot begins a tick while more than this many ticks are pushed and
+ *     not landed (a quarter second of ticks is the reference's bound), the domain freezes as it
+ *     stands: each queued tick is then dropped, one a slot (its events applied in order, no
+ *     sub-step, landed with `dropped` set), and counted, until the queue has drained; then it
+ *     thaws, and the next tick pushed steps as before;
+ *   - max_slots: the most slots one call enqueues (a frame's ceiling, `water_live.frame.max_slots`);
+ *     a call that asks for more enqueues max_slots.
+ * Waits for the device; call it between slots. */
+int wl_queue_set_limits(wl_queue* queue, uint32_t lag_limit_ticks, uint32_t max_slots, char* err,
+                        size_t err_len);
 /* `slots` slots on `stream` (null: the step's own stream), no wait; graph-capturable. */
 int wl_queue_enqueue_slots(wl_queue* queue, wl_stream stream, uint32_t slots);
 /* The slots, then a wait. */

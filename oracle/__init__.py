@@ -73,6 +73,7 @@ def lib():
             ("oracle_step_set_source", [C.c_void_p, _dp, C.c_uint32, C.c_int]),
             ("oracle_step_run_steps", [C.c_void_p, C.c_uint32, C.c_double]),
             ("oracle_step_run_length_pass", [C.c_void_p, C.c_double]),
+            ("oracle_step_prime", [C.c_void_p]),
             ("oracle_step_read_ledger", [C.c_void_p, _dp]),
             ("oracle_step_read_state_f32", [C.c_void_p, _fp]),
             ("oracle_step_read_state_f64", [C.c_void_p, _dp]),
@@ -232,6 +233,10 @@ class RefStep:
 
     def run_length_pass(self, max_dt):
         lib().oracle_step_run_length_pass(self.h, float(max_dt))
+
+    def prime(self):
+        """prime_main: the records of the state as it stands (slang:373-386)."""
+        lib().oracle_step_prime(self.h)
 
     def read_ledger(self):
         out = np.zeros(6)

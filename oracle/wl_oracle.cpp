@@ -132,6 +132,12 @@ void oracle_step_read_state_f64(void* p, double* out) {
   std::memcpy(out, s->f64.planes(), sizeof(double) * k_state_planes * s->f64.n);
 }
 
+void oracle_step_prime(void* p) {  // prime_main (slang:373-386) of the state as it stands
+  auto* s = static_cast<StepHandle*>(p);
+  if (s->is64) s->f64.prime_records();
+  else s->f32.prime_records();
+}
+
 void oracle_step_write_planes_f32(void* p, const float* planes) {  // a raw upload, for the tests
   auto* s = static_cast<StepHandle*>(p);
   std::memcpy(s->f32.planes_mut(), planes, sizeof(float) * k_state_planes * s->f32.n);

@@ -391,6 +391,8 @@ class RefStep {
   }
 
   void run_length_pass(T max_dt) { dt_main(max_dt); }  // water_live.cpp:415-437
+  // prime_main (slang:373-386) of the state as it stands: the records of a state just written.
+  void prime_records() { prime(); }
 
   // advance (water_live.cpp:594-632): batches of 64 steps of unlimited length until the time
   // kept in T has run out; the steps after it choose a length of zero.

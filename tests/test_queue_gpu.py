@@ -14,8 +14,8 @@ import pytest
 
 import cases
 from pairs import bits, make_pair
-from game_engine_gb300.tick_queue import (EVENT_BED, EVENT_MANNING, EVENT_SOURCE, ERR_REFUSED,
-                                          Event, TickQueue)
+from game_engine_gb300.tick_queue import (EVENT_BED, EVENT_MANNING, EVENT_SOURCE, EVENT_STATE,
+                                          ERR_REFUSED, Event, TickQueue)
 
 pytestmark = pytest.mark.gpu
 TICK = float(np.float32(1.0 / 60.0))
@@ -61,15 +61,38 @@ def oracle_run(ref, c, plan, compensate=False):
     for _, length, events in plan:
         for e in events:
             v = np.asarray(e.values, np.float32)
+            if e.kind == EVENT_STATE:
+                oracle_state_event(ref, nx, ny, e)
+                continue
             p = planes[e.kind].reshape(ny, nx)
             p[e.y0:e.y0 + v.shape[0], e.x0:e.x0 + v.shape[1]] = v
-        for kind in {e.kind for e in events}:
+        for kind in {e.kind for e in events} - {EVENT_STATE}:
             wide = planes[kind].astype(np.float64)  # f32 values widen exactly; datum 0
             {EVENT_BED: lambda: ref.set_bed(wide, 0.0),
              EVENT_SOURCE: lambda: ref.set_source(wide, 1, compensate),
              EVENT_MANNING: lambda: ref.set_manning(wide)}[kind]()
         steps.append(ref.advance(length)[0] if length > 0 else 0)
     return steps
+
+
+def oracle_state_event(ref, nx, ny, e):
+    """A state event in the oracle: the flush (dt_main with max_dt 0), the rectangle's h, hu, hv
+    written and its remainder zeroed, then prime_main of the new state."""
+    ref.run_length_pass(0.0)
+    planes = ref.read_state_bits().reshape(4, ny, nx).copy()
+    v = np.asarray(e.values, np.float32)
+    h, w = v.shape[-2:]
+    planes[0:3, e.y0:e.y0 + h, e.x0:e.x0 + w] = v
+    planes[3, e.y0:e.y0 + h, e.x0:e.x0 + w] = 0.0
+    ref.write_planes(planes.ravel())
+    ref.prime()
+
+
+def lake_patch(c, x0, y0, w, h, level):
+    """A rectangle of a lake at rest at `level` over the case's bed: (3, h, w) values."""
+    bed = np.asarray(c["bed"], np.float64).astype(np.float32).reshape(c["ny"], c["nx"])
+    depth = np.maximum(np.float32(level) - bed[y0:y0 + h, x0:x0 + w], 0.0)
+    return np.stack([depth, np.zeros_like(depth), np.zeros_like(depth)])
 
 
 def device_run(q, n_ticks, partition, most_calls=20000):
@@ -117,7 +140,8 @@ def test_queued_ticks_equal_advance_per_tick(gpu, case, partition):
         if r["substeps"]:
             assert 0.0 < r["shortest_s"] <= r["longest_s"] <= TICK
     st = q.status()
-    assert st == dict(pushed=n, begun=n, landed=n, active=0, substeps=st["substeps"])
+    assert st == dict(pushed=n, begun=n, landed=n, active=0, substeps=st["substeps"], dropped=0,
+                      frozen=0, freezes=0)
     # Idle slots change nothing.
     h = dev.state_hash()
     assert q.run_slots(9), q.error
@@ -304,4 +328,132 @@ def test_queued_ticks_in_the_other_forms(gpu, form):
     device_run(q, n, [2, 3])
     assert_same_after_ticks(dev, ref, form)
     assert [r["substeps"] for r in q.landed(0, n)] == want
+    q.close()
+
+
+@pytest.mark.parametrize("case", ["slope", "basin"])
+@pytest.mark.parametrize("partition", [[1], [3, 1, 7, 2]])
+def test_a_state_event_wakes_the_tile_at_its_tick(gpu, case, partition):
+    """The apply pass's waking state (water_live.md:80, ADR-0080 decision 4): lakes at rest written
+    over rectangles at two ticks' boundaries, among the plan's other events, one of them in a tick
+    of no length; the bytes equal the oracle's flush, write and prime between its advances."""
+    c = cases.slope(False) if case == "slope" else cases.closed_basin()
+    dev, ref = make_pair(c)
+    n = 16
+    plan = plan_for(c, n, seed=29)
+    t, length, events = plan[4]
+    plan[4] = (t, length, events + [Event(EVENT_STATE, 3, 2, lake_patch(c, 3, 2, 20, 11, 0.45))])
+    t, length, events = plan[9]  # a tick of no length
+    plan[9] = (t, length, [Event(EVENT_STATE, 0, 0, lake_patch(c, 0, 0, c["nx"], 5, 0.3))] + events)
+    want = oracle_run(ref, c, plan)
+    q = TickQueue(dev, records=32, arena_values=1 << 14, max_events=64)
+    for p in plan:
+        assert q.push(*p), q.error
+    device_run(q, n, partition)
+    assert_same_after_ticks(dev, ref, f"{case} state events")
+    assert [r["substeps"] for r in q.landed(0, n)] == want
+    q.close()
+
+
+def test_a_batch_tile_wakes_from_its_baked_answer(gpu):
+    """A domain of uneven tiles; at tick 3 tile 2 is woken with the baked answer (a lake at rest
+    over its whole bed) by a state event while the others step on: every tile equals its oracle."""
+    from game_engine_gb300.batch import Batch
+    from test_batch_gpu import load, mixed_tiles
+    import oracle
+    tiles, sides, edges = mixed_tiles()
+    b = Batch(sides, open_edges=edges)
+    load(b, tiles)
+    refs = []
+    for k, t in enumerate(tiles):
+        r = oracle.RefStep(oracle.Grid(t.nx, t.ny, t.cell_m, open_edges=edges[k]))
+        r.set_bed(t.bed)
+        r.set_source(t.source)
+        r.write_state(t.h, t.hu, t.hv)
+        refs.append(r)
+    k2 = 2
+    t2 = tiles[k2]
+    c2 = dict(nx=t2.nx, ny=t2.ny, bed=t2.bed)
+    wake = Event(EVENT_STATE, 0, 0, lake_patch(c2, 0, 0, t2.nx, t2.ny, 2.2), tile=k2)
+    plan = [(tick, TICK, [wake] if tick == 3 else []) for tick in range(9)]
+    for tick, length, events in plan:
+        for e in events:
+            oracle_state_event(refs[e.tile], *sides[e.tile], e)
+        for r in refs:
+            r.advance(length)
+    q = TickQueue(b, records=16, arena_values=1 << 16)
+    for p in plan:
+        assert q.push(*p), q.error
+    device_run(q, len(plan), [2, 1])
+    ledgers = b.ledgers()
+    for k, r in enumerate(refs):
+        got, exp = b.read_tile_bits(k), r.read_state_bits()
+        assert np.array_equal(got.view(np.uint32), exp.view(np.uint32)), f"tile {k} {sides[k]}"
+        led = r.read_ledger()
+        for key in LEDGER_SUMS:
+            assert ledgers[k][key] == led[key], (k, key)
+    q.close()
+    b.close()
+
+
+def test_a_lagging_domain_freezes_drops_and_thaws(gpu):
+    """The lag control (water_live.md:90-92): with a lag limit of 4 ticks, three ticks step as
+    ever; eight pushed at once put the lag past the limit, so the domain freezes as it stands and
+    drops all eight, one a slot, applying their events in order (two overlapping bed patches and
+    a waking state among them) and counting them; the landing that drains the queue thaws it, and
+    the next two ticks step again. The bytes equal the oracle's run of the same ticks with the
+    dropped ones' events applied and no advance."""
+    c = cases.slope(False)
+    dev, ref = make_pair(c)
+    q = TickQueue(dev, records=16, arena_values=1 << 14, max_events=64)
+    assert q.set_limits(4, 0), q.error
+    first = [(t, TICK, []) for t in range(3)]
+    burst = [(10 + t, TICK, []) for t in range(8)]
+    burst[1] = (11, TICK, [Event(EVENT_BED, 2, 2, np.full((3, 3), 0.15))])
+    burst[4] = (14, TICK, [Event(EVENT_BED, 3, 3, np.full((3, 3), 0.25)),
+                           Event(EVENT_STATE, 5, 1, lake_patch(c, 5, 1, 12, 8, 0.5))])
+    last = [(30 + t, TICK, []) for t in range(2)]
+    want_first = oracle_run(ref, c, first)
+    for p in first:
+        assert q.push(*p), q.error
+    device_run(q, 3, [2])
+    st = q.status()
+    assert (st["dropped"], st["frozen"], st["freezes"]) == (0, 0, 0)
+    oracle_run(ref, c, [(t, 0.0, e) for t, _, e in burst])  # the dropped ticks: events alone
+    for p in burst:
+        assert q.push(*p), q.error
+    device_run(q, 11, [3, 1])
+    st = q.status()
+    assert (st["dropped"], st["frozen"], st["freezes"]) == (8, 0, 1)
+    rec = q.landed(3, 8)
+    assert [r["dropped"] for r in rec] == [1] * 8
+    assert [r["substeps"] for r in rec] == [0] * 8
+    assert [r["dropped_total"] for r in rec] == list(range(1, 9))
+    assert rec[0]["lag"] == 8 and [r["frozen"] for r in rec] == [1] * 7 + [0]
+    assert [r["events"] for r in rec] == [len(e) for _, _, e in burst]
+    want_last = oracle_run(ref, c, last)
+    for p in last:
+        assert q.push(*p), q.error
+    device_run(q, 13, [1])
+    rec = q.landed(11, 2)
+    assert [r["dropped"] for r in rec] == [0, 0]
+    assert [r["substeps"] for r in rec] == want_last
+    assert [r["substeps"] for r in q.landed(0, 3)] == want_first
+    assert_same_after_ticks(dev, ref, "frozen and thawed")
+    q.close()
+
+
+def test_max_slots_caps_a_call(gpu):
+    dev, _ = make_pair(cases.closed_basin())
+    q = TickQueue(dev, records=16)
+    assert q.set_limits(0, 3), q.error
+    for t in range(10):
+        assert q.push(t, TICK), q.error
+    before = int(dev.read_ledger_bits()[10])
+    assert q.run_slots(100), q.error
+    taken = int(dev.read_ledger_bits()[10]) - before
+    assert taken == 3  # three slots, each a sub-step of a tick in flight
+    assert q.set_limits(0, 0), q.error
+    assert q.run_slots(5), q.error
+    assert int(dev.read_ledger_bits()[10]) - before == 8
     q.close()
