@@ -42,6 +42,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L2_FLUSH_BYTES = 512 << 20  # larger than the GB300's L2 (129 MB)
+CONFIGS_GOLDEN = os.path.join(ROOT, "tests", "golden", "configs.json")
+
+
+def golden_config(name):
+    """The oracle's answer for a configuration at full size (tests/golden/make_configs.py), or
+    None where the fixture is absent."""
+    try:
+        with open(CONFIGS_GOLDEN) as f:
+            return json.load(f).get(name)
+    except OSError:
+        return None
 
 
 def peaks():
@@ -243,6 +254,12 @@ def run_plain(args, tile, rank, world):
             flush_l2()
         torch.cuda.synchronize(dev)
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    # Untimed: the last step's state against the oracle's hash of the same ticks.
+    gold = golden_config(tile.meta.get("name"))
+    oracle_equal = None
+    if gold is not None and gold.get("ticks") == ticks and gold.get("max_dt") == max_dt:
+        oracle_equal = step.state_hash() == gold["hash"]
+        assert oracle_equal, "the timed run's state differs from the oracle's (state hash)"
     from game_engine_gb300.shard import max_over_ranks
     ms = max_over_ranks(ms)  # the slowest rank's time (gloo or NCCL group under torchrun)
     launches = args.steps * (ticks + 2)
@@ -317,6 +334,7 @@ def run_plain(args, tile, rank, world):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "state_hash_equals_oracle": oracle_equal,
     }
     return out
 
@@ -354,6 +372,14 @@ def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
         torch.cuda.synchronize(dev)
         ms += ev[0].elapsed_time(ev[1])
     batched = cells * ticks * steps / (ms * 1e-3)
+    # Untimed: every tile's state after the last step's ticks against the oracle's hashes.
+    gold = golden_config("tiles_4096")
+    hashes_equal = None
+    if gold is not None and gold["count"] == count and gold["ticks"] == ticks:
+        got = [int(h) for h in b.tile_hashes()]
+        hashes_equal = got == gold["hashes"]
+        assert hashes_equal, (f"{sum(a != w for a, w in zip(got, gold['hashes']))} of {count} "
+                              "tiles differ from the oracle's hashes")
     # The per-tile-launch form on the same tiles, timed four ways: 16-row marches on one stream,
     # from a captured graph, and dealt to 64 concurrent streams as independent steps would run;
     # and the three-phase blocks (the small-tile shape) on 64 streams. The best of them is the
@@ -381,6 +407,7 @@ def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
         "per_tile_launch": {"value": per_tile, "unit": "cell-updates/s", "forms": per,
                             "best": max(per, key=per.get)},
         "speedup_vs_per_tile_launch": batched / per_tile,
+        "tile_hashes_equal_oracle": hashes_equal,
         "launches_per_tick": {"batched": 1, "per_tile": count},
     }
 

@@ -186,16 +186,22 @@ def tile_sides(count: int, seed: int, sides=TILE_SIDES):
 
 
 def tiles_4096(count: int = 4096, sides=None, seed: int | None = None, with_bed: bool = True,
-               terrain=fbm):
-    """The batched workload: `count` tiles of seeded sides, each its own fBm and 2 m column."""
+               terrain=fbm, only=None):
+    """The batched workload: `count` tiles of seeded sides, each its own fBm and 2 m column.
+    `only`: build just these tile indices (the list holds None elsewhere; the seeded draws are the
+    same)."""
     seed = SEEDS["tiles_4096"] if seed is None else seed
     sides = tile_sides(count, seed) if sides is None else sides
+    keep = None if only is None else set(only)
     rng = np.random.Generator(np.random.PCG64((seed >> 32) & 0xFFFFFFFF))
     out = []
     for k, s in enumerate(sides):
-        bed = terrain(s, s, 20.0, seed + 7919 * (k + 1)) if with_bed else np.zeros(s * s)
         x0 = int(rng.integers(0, s - 32 + 1))
         y0 = int(rng.integers(0, s - 32 + 1))
+        if keep is not None and k not in keep:
+            out.append(None)
+            continue
+        bed = terrain(s, s, 20.0, seed + 7919 * (k + 1)) if with_bed else np.zeros(s * s)
         out.append(Tile(s, s, bed, column(s, s, x0, y0), meta=dict(index=k)))
     return out
 
@@ -236,11 +242,16 @@ def adjoint_512(side: int = 512, terrain=fbm) -> Tile:
 ADJOINT_TILE_SIDES = (64, 128, 192, 256, 320, 384, 448, 512)
 
 
-def tiles_256_adjoint(count: int = 256, terrain=fbm) -> list:
+def tiles_256_adjoint(count: int = 256, terrain=fbm, only=None) -> list:
+    """`only`: build just these tile indices (None elsewhere), as tiles_4096."""
     seed = SEEDS["tiles_256_adjoint"]
     sides = tile_sides(count, seed, ADJOINT_TILE_SIDES)
+    keep = None if only is None else set(only)
     out = []
     for k, s in enumerate(sides):
+        if keep is not None and k not in keep:
+            out.append(None)
+            continue
         bed = terrain(s, s, ADJOINT_RELIEF_M, seed + 7919 * (k + 1))
         out.append(Tile(s, s, bed, lake(s, s, bed, ADJOINT_LEVEL_M, ADJOINT_RISE_M, phase=0.1 * k),
                         source=np.zeros(s * s),

@@ -14,8 +14,8 @@ themselves to the oracle, not only smaller cases of the same code:
                      gradient's largest magnitude.
 
 Terrain comes from workloads.fbm_numpy (the same doubles as the library's generator), so nothing
-here loads the CUDA library. Work is dealt to processes (spawn) by tile. About 25 minutes on 8
-cores.
+here loads the CUDA library. Work is dealt to processes (spawn) by tile, each building only the
+tiles it steps. About 25 minutes on 8 cores.
 
     python tests/golden/make_configs.py [--only plain_2048,tiles_4096,tiles_256_adjoint]
 """
@@ -36,22 +36,6 @@ import numpy as np  # noqa: E402
 
 OUT = os.path.join(HERE, "configs.json")
 GRAD_CELLS = 32
-
-
-class _SomeTerrain:
-    """fbm_numpy for the tiles first .. last - 1 of a workload's list (its calls come in tile
-    order) and a flat bed for the rest, so that a process builds only the terrain it steps."""
-
-    def __init__(self, first, last):
-        self.first, self.last, self.k = first, last, 0
-
-    def __call__(self, nx, ny, height, seed):
-        from game_engine_gb300 import workloads as W
-        k = self.k
-        self.k += 1
-        if self.first <= k < self.last:
-            return W.fbm_numpy(nx, ny, height, seed)
-        return np.zeros(nx * ny)
 
 
 def _plain_2048():
@@ -76,7 +60,7 @@ def _tiles_4096_part(args):
     first, last = args
     import oracle
     from game_engine_gb300 import workloads as W
-    tiles = W.tiles_4096(terrain=_SomeTerrain(first, last))
+    tiles = W.tiles_4096(terrain=W.fbm_numpy, only=range(first, last))
     out = []
     for k in range(first, last):
         t = tiles[k]
@@ -91,7 +75,7 @@ def _tiles_4096_part(args):
 def _adjoint_tile(k):
     import oracle
     from game_engine_gb300 import workloads as W
-    t = W.tiles_256_adjoint(terrain=_SomeTerrain(k, k + 1))[k]
+    t = W.tiles_256_adjoint(terrain=W.fbm_numpy, only=[k])[k]
     seed = W.SEEDS["tiles_256_adjoint"]
     ticks, dt = W.TILES_ADJOINT_TICKS, W.MAX_DT
     g = oracle.Grid(t.nx, t.ny, t.cell_m)
