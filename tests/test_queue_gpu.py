@@ -308,8 +308,8 @@ def test_a_batch_queue_equals_advance_per_tile(gpu, rows):
 
 @pytest.mark.parametrize("form", ["fixed", "stored_faces", "compensate"])
 def test_queued_ticks_in_the_other_forms(gpu, form):
-    """The fixed arithmetic, the stored-faces form and the compensated source through the queue:
-    the same bytes as the oracle's advance per tick."""
+    """The fixed arithmetic, the stored-faces form and the compensated source through the queue,
+    a waking state among the events: the same bytes as the oracle's advance per tick."""
     c = cases.slope(False)
     kw = {"fixed": dict(fixed=True), "stored_faces": dict(stored_faces=True),
           "compensate": dict(compensate=True)}[form]
@@ -320,6 +320,9 @@ def test_queued_ticks_in_the_other_forms(gpu, form):
         # a source event resets nothing of the remainder: the oracle's set_source would, so the
         # plan carries bed events alone
         plan = [(t, l, [e for e in ev if e.kind == EVENT_BED]) for t, l, ev in plan]
+    # a waking state at tick 6 in every form (in the compensated one its remainder is zeroed)
+    t6, l6, e6 = plan[6]
+    plan[6] = (t6, l6, e6 + [Event(EVENT_STATE, 4, 3, lake_patch(c, 4, 3, 15, 9, 0.4))])
     oracle_run_kw = dict(compensate=True) if form == "compensate" else {}
     want = oracle_run(ref, c, plan, **oracle_run_kw)
     q = TickQueue(dev, records=16)
