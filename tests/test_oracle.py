@@ -159,3 +159,21 @@ def test_solver64_thread_count_invariance(oracle_mod):
         s.advance(5.0)
         hashes.append(s.state_hash())
     assert hashes[0] == hashes[1] == hashes[2] != 0
+
+
+def test_prime_of_a_raw_upload_equals_write_state(oracle_mod):
+    # The oracle's state event (flush, raw write, prime) leaves the records that write_state's own
+    # prime leaves for the same planes: prime_main depends on the state alone.
+    c = cases.slope(False)
+    a = refstep(oracle_mod, c)
+    a.run_steps(30, 0.01)
+    planes = a.read_state_bits().copy()
+    a.run_length_pass(0.0)
+    a.write_planes(planes)
+    a.prime()
+    b = refstep(oracle_mod, c)
+    n = c["nx"] * c["ny"]
+    b.write_state(planes[:n].astype(np.float64), planes[n:2 * n].astype(np.float64),
+                  planes[2 * n:3 * n].astype(np.float64))
+    assert np.array_equal(a.read_partials_bits().view(np.uint32),
+                          b.read_partials_bits().view(np.uint32))
