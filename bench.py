@@ -140,10 +140,33 @@ def cpu_baseline(tile, threads: int, budget_s: float = 12.0):
     for _ in range(ticks):
         s.step(max_dt)
     dt = time.perf_counter() - t0
-    return {"value": tile.cells * ticks / dt, "unit": "cell-updates/s", "cores": threads,
-            "kind": "port",
-            "sample": f"{ticks} ticks of the {tile.nx}x{tile.ny} tile (after 1 untimed), FP64 "
-                      f"reference CPU tick restated in oracle/, {threads} threads"}
+    out = {"value": tile.cells * ticks / dt, "unit": "cell-updates/s", "cores": threads,
+           "kind": "port",
+           "sample": f"{ticks} ticks of the {tile.nx}x{tile.ny} tile (after 1 untimed), FP64 "
+                     f"reference CPU tick restated in oracle/, {threads} threads"}
+    # Beside it, bounded samples of the same tick on one thread, and of the FP32 restatement of
+    # the card's step (the oracle the GPU tick is held to) on one core.
+    one = oracle.Solver64(g, 1)
+    one.set_state(tile.h, tile.hu, tile.hv)
+    one.set_inputs(tile.bed, None, tile.source)
+    t0, n1 = time.perf_counter(), 0
+    while time.perf_counter() - t0 < budget_s / 4 and n1 < 50:
+        one.step(max_dt)
+        n1 += 1
+    out["one_thread"] = {"value": tile.cells * n1 / (time.perf_counter() - t0),
+                         "unit": "cell-updates/s", "ticks": n1}
+    r = oracle.RefStep(oracle.Grid(tile.nx, tile.ny, tile.cell_m))
+    r.set_bed(tile.bed)
+    if tile.source is not None:
+        r.set_source(tile.source)
+    r.write_state(tile.h, tile.hu, tile.hv)
+    t0, n2 = time.perf_counter(), 0
+    while time.perf_counter() - t0 < budget_s / 4 and n2 < 50:
+        r.run_steps(1, max_dt)
+        n2 += 1
+    out["fp32_oracle_one_core"] = {"value": tile.cells * n2 / (time.perf_counter() - t0),
+                                   "unit": "cell-updates/s", "ticks": n2}
+    return out
 
 
 def workload_config(tile, ticks: int, world: int) -> dict:
