@@ -11,7 +11,10 @@ themselves to the oracle, not only smaller cases of the same code:
                      from the oracle's FP32 run on the perturbed bed, then the oracle's FP32
                      reverse sweep: the loss, and the gradients with respect to the bed and the
                      source at the tile's 64 probe cells and at 32 seeded cells, with each
-                     gradient's largest magnitude.
+                     gradient's largest magnitude;
+  tiles_256_adjoint_fd  for four of those tiles (sides 64, 128, 192 and 256), central differences
+                     of the FP64 replay's loss at 8 cells each, on the bed (eps 1e-3 m) and the
+                     source (1e-3 relative), at cells drawn away from bed ties.
 
 Terrain comes from workloads.fbm_numpy (the same doubles as the library's generator), so nothing
 here loads the CUDA library. Work is dealt to processes (spawn) by tile, each building only the
@@ -101,9 +104,41 @@ def _adjoint_tile(k):
                    g_bed_max=float(np.abs(g_bed).max()), g_src_max=float(np.abs(g_src).max()))
 
 
+FD_TILES = (2, 10, 3, 0)  # sides 64, 128, 192, 256
+FD_CELLS = 8
+
+
+def _adjoint_fd_tile(k):
+    import oracle
+    sys.path.insert(0, os.path.dirname(HERE))
+    from adjoint_cases import fd_cells
+    from game_engine_gb300 import workloads as W
+    t = W.tiles_256_adjoint(terrain=W.fbm_numpy, only=[k])[k]
+    seed = W.SEEDS["tiles_256_adjoint"]
+    ticks, dt = W.TILES_ADJOINT_TICKS, W.MAX_DT
+    g = oracle.Grid(t.nx, t.ny, t.cell_m)
+    tgt = oracle.RefStep(g)
+    tgt.set_bed(W.perturbed_bed(t.bed, seed + k))
+    tgt.set_source(t.source)
+    tgt.write_state(t.h, t.hu, t.hv)
+    tgt.run_steps(ticks, dt)
+    probes = t.meta["probes"]
+    targets = tgt.read_state_bits()[:t.cells][probes].astype(np.float64)
+    state0 = np.concatenate([t.h, t.hu, t.hv])
+    cells = fd_cells(dict(nx=t.nx, ny=t.ny, bed=t.bed), FD_CELLS, seed=(seed + k) & 0xFFFF,
+                     eps=1e-3)
+    fd_bed, fd_src = oracle.adj_fd(g, dt, ticks, t.bed, t.source, state0, probes, targets, cells,
+                                   eps_bed=1e-3, rel_source=1e-3, threads=1)
+    loss64 = oracle.adj_loss64(g, dt, ticks, t.bed, t.source, state0, probes, targets)
+    return k, dict(index=k, nx=t.nx, ny=t.ny, cells=[int(c) for c in cells], loss_fp64=loss64,
+                   fd_bed=[float(v) for v in fd_bed], fd_src=[float(v) for v in fd_src],
+                   eps_bed=1e-3, rel_source=1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="plain_2048,tiles_4096,tiles_256_adjoint")
+    ap.add_argument("--only",
+                    default="plain_2048,tiles_4096,tiles_256_adjoint,tiles_256_adjoint_fd")
     ap.add_argument("--procs", type=int, default=os.cpu_count() or 1)
     args = ap.parse_args()
     import oracle
@@ -127,6 +162,8 @@ def main():
                                                       for a in range(0, 4096, step)])
         if "tiles_256_adjoint" in only:
             adj = pool.map_async(_adjoint_tile, range(256))
+        if "tiles_256_adjoint_fd" in only:
+            fd = pool.map_async(_adjoint_fd_tile, FD_TILES)
         t0 = time.time()
         if "tiles_4096" in only:
             hashes = [0] * 4096
@@ -139,6 +176,9 @@ def main():
             out["tiles_256_adjoint"] = dict(count=256, ticks=500, every=25, max_dt=0.01,
                                             tiles=[r for _, r in res])
             print(f"tiles_256_adjoint done at {time.time() - t0:.0f} s", flush=True)
+        if "tiles_256_adjoint_fd" in only:
+            out["tiles_256_adjoint_fd"] = [r for _, r in fd.get()]
+            print(f"tiles_256_adjoint_fd done at {time.time() - t0:.0f} s", flush=True)
         if "plain_2048" in only:
             out["plain_2048"] = jobs["plain_2048"].get()
             print(f"plain_2048 done at {time.time() - t0:.0f} s", flush=True)

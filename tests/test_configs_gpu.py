@@ -8,7 +8,8 @@ restatement of the card's step, on the CPU):
   - the 256-tile batched adjoint (500 ticks, a checkpoint every 25): each tile's loss, and its
     gradients with respect to the bed and the source at its 64 probes and 32 seeded cells, within
     1e-5 of the tile's largest gradient (the reverse sweep's derivative-only arithmetic takes
-    fast reciprocals and contraction; its forward is bit-exact).
+    fast reciprocals and contraction; its forward is bit-exact); and on four tiles, against the
+    FP64 replay's central differences within 1e-4.
 """
 from __future__ import annotations
 
@@ -24,6 +25,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "configs.json")
 ADJOINT_TOL = 1e-5
+FD_TOL = 1e-4
 
 
 def golden():
@@ -92,5 +94,17 @@ def test_tiles_256_adjoint_losses_and_gradients(gpu):
                 worst = max(worst, err)
                 assert err < ADJOINT_TOL, (k, key, where, err)
     print(f"tiles_256_adjoint: worst gradient error {worst:.2e} of each tile's largest")
+    # Against the FP64 replay's central differences on four tiles (the benchmark spec's bound, 1e-4
+    # of the largest difference at the tile's cells).
+    from adjoint_cases import rel_err
+    for r in golden()["tiles_256_adjoint_fd"]:
+        k = r["index"]
+        sl = b.tile_slice(k)
+        cells = np.array(r["cells"])
+        assert loss[k] == pytest.approx(r["loss_fp64"], rel=1e-3), k
+        err_bed = rel_err(g_bed[sl][cells], r["fd_bed"])
+        err_src = rel_err(g_src[sl][cells], r["fd_src"])
+        print(f"tile {k} ({r['nx']}x{r['ny']}): bed {err_bed:.2e}, source {err_src:.2e} of FD")
+        assert err_bed < FD_TOL and err_src < FD_TOL, (k, err_bed, err_src)
     a.close()
     b.close()

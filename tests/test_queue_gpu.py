@@ -443,6 +443,16 @@ def test_a_lagging_domain_freezes_drops_and_thaws(gpu):
     assert [r["substeps"] for r in rec] == want_last
     assert [r["substeps"] for r in q.landed(0, 3)] == want_first
     assert_same_after_ticks(dev, ref, "frozen and thawed")
+    # A second burst freezes the domain again; the drops add up across freezes.
+    again = [(40 + t, TICK, [Event(EVENT_BED, t, 0, np.full((1, 2), 0.05 * t))]) for t in range(6)]
+    oracle_run(ref, c, [(t, 0.0, e) for t, _, e in again])
+    for p in again:
+        assert q.push(*p), q.error
+    device_run(q, 19, [4])
+    st = q.status()
+    assert (st["dropped"], st["frozen"], st["freezes"]) == (14, 0, 2)
+    assert [r["dropped_total"] for r in q.landed(13, 6)] == list(range(9, 15))
+    assert_same_after_ticks(dev, ref, "frozen twice")
     q.close()
 
 
