@@ -269,6 +269,7 @@ def run_plain(args, tile, rank, world):
         dist.barrier()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    tick_launches0 = step.tick_launches()
     with Clocks(dev) as clocks:
         for k in range(args.steps):
             starts[k].record(stream)
@@ -277,6 +278,7 @@ def run_plain(args, tile, rank, world):
             flush_l2()
         torch.cuda.synchronize(dev)
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    tick_launches = step.tick_launches() - tick_launches0
     # Untimed: the last step's state against the oracle's hash of the same ticks.
     gold = golden_config(tile.meta.get("name"))
     oracle_equal = None
@@ -285,11 +287,13 @@ def run_plain(args, tile, rank, world):
         assert oracle_equal, "the timed run's state differs from the oracle's (state hash)"
     from game_engine_gb300.shard import max_over_ranks
     ms = max_over_ranks(ms)  # the slowest rank's time (gloo or NCCL group under torchrun)
-    launches = args.steps * (ticks + 2)
+    # A step: the restore and the prime, then the ticks (one resident launch for a small tile).
+    launches = args.steps * 2 + tick_launches
 
     # The dominant kernel's average launch, from the same events: every launch of a step but two
     # (the restore and the prime, a few microseconds) is a tick, enqueued ahead of the device, so
-    # a step's time over its ticks is the tick's duration with the gap between launches included.
+    # a step's time over its ticks is the tick's duration with the gap between launches included
+    # (a small tile's resident launch: its ticks' share of the launch, bytes and time alike).
     tick_ms = ms / args.steps / ticks
     bytes_per_cell = 28.0 + (4.0 if tile.source is not None else 0.0) + 32.0 / 256.0
     algo_bytes = bytes_per_cell * n

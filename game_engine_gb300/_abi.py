@@ -126,6 +126,8 @@ SIGNATURES = {
     "wl_valid": (C.c_int, [C.c_void_p]),
     "wl_cell_count": (C.c_uint32, [C.c_void_p]),
     "wl_group_count": (C.c_uint32, [C.c_void_p]),
+    "wl_tick_launches": (C.c_uint64, [C.c_void_p]),
+    "wl_resident_barrier_check": (C.c_int, [C.c_int, C.c_uint32, C.c_char_p, C.c_size_t]),
     "wl_write_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
     "wl_read_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
     "wl_read_state_bits": (C.c_int, [C.c_void_p, _fp, C.c_size_t, *_err]),

@@ -162,6 +162,10 @@ uint32_t wl_cell_count(const wl_step* step) { return valid(step) ? step->cells :
 
 uint32_t wl_group_count(const wl_step* step) { return valid(step) ? step->groups : 0u; }
 
+uint64_t wl_tick_launches(const wl_step* step) {
+  return valid(step) ? step->set.tick_launches() : 0u;
+}
+
 int wl_write_state(wl_step* s, const double* h, const double* hu, const double* hv, size_t n,
                    char* err, size_t err_len) {
   if (!valid(s)) return fail(err, err_len, WL_ERR_INVALID, k_no_device);
@@ -388,6 +392,34 @@ int wl_run_length_pass(wl_step* s, float max_dt, char* err, size_t err_len) {
 uint64_t wl_hash_floats(const float* values, size_t count) {
   if (values == nullptr) count = 0;
   return wlc::fnv1a_floats(values, count);
+}
+
+int wl_resident_barrier_check(int device, uint32_t ctas, char* err, size_t err_len) {
+  if (ctas < 2 || ctas > 64) return fail(err, err_len, WL_ERR_INVALID, "water_live: 2 to 64 CTAs");
+  if (cudaSetDevice(device) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaSetDevice");
+  wlc::ResidentCtl* rc = nullptr;
+  if (cudaMalloc(&rc, sizeof(wlc::ResidentCtl)) != cudaSuccess)
+    return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaMalloc");
+  cudaStream_t s = nullptr;
+  int rc_out = WL_OK;
+  wlc::ResidentCtl word = {};
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      wlc::launch_barrier_probe(rc, ctas, s) != cudaSuccess) {
+    rc_out = fail(err, err_len, WL_ERR_CUDA, std::string("water_live: the barrier probe: ") +
+                                                 cudaGetErrorString(cudaGetLastError()));
+  } else {
+    bool timed_out = false;
+    const cudaError_t e = wlc::wait_stream(s, &timed_out);
+    if (timed_out || e != cudaSuccess ||
+        cudaMemcpy(&word, rc, sizeof word, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc_out = fail(err, err_len, WL_ERR_CUDA, "water_live: the barrier probe did not finish");
+    else if (word.error == 0u || word.arrived != ctas - 1u)
+      rc_out = fail(err, err_len, WL_ERR_CUDA, "water_live: the barrier's wait did not give up");
+  }
+  if (s != nullptr) cudaStreamDestroy(s);
+  cudaFree(rc);
+  return rc_out;
 }
 
 wl_stream wl_step_stream(wl_step* s) {

@@ -96,6 +96,24 @@ struct WorkCtl {
   uint32_t pad;
 };
 
+// The resident tick's words (one a tile set, zeroed before each resident launch): the grid
+// barrier's arrivals (a CTA adds one a tick) and its error word, and three rotating slots of what a
+// tick reads from the last one: the largest speeds of its update and the ledger's time left. In
+// three slots nothing waits at the barrier for a slot to be cleared, and a tick reads its slot in
+// one 16-byte load.
+struct ResidentSlot {
+  uint32_t max_a, max_b;
+  float remaining_s;
+  uint32_t pad;
+};
+struct ResidentCtl {
+  uint32_t arrived;
+  uint32_t error;
+  uint32_t pad[2];
+  ResidentSlot slot[3];
+};
+static_assert(sizeof(ResidentCtl) == 64, "ResidentCtl layout");
+
 // ---- dependent launches ---------------------------------------------------------------------
 //
 // The tick, the queue's slot and the adjoint's sweeps are launched as programmatic dependents of

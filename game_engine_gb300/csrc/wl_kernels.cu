@@ -197,20 +197,12 @@ __device__ void ledger_update(LedgerBits& l, float src, float opn, float rnd, fl
   }
 }
 
-// The end of a work item (one thread): its largest speeds into slot rec ^ 1 of the tile's maxima
-// and, for the tile's last item, the flip. No fence: the item's planes, records and maxima are
-// read by the next launch, and the flip reads only fields no other item writes. Every other item
-// of the tile has read slot `rec` (its step's length) before its count, so the last item may clear
-// it. A tick also flips the copy and moves the source's clock; a prime flips only the records.
-// `extra` counts a CTA that folded the ledger apart from the items (1) or none (0).
-__device__ void finish_item(const TileDesc& T, uint32_t rec, uint32_t amax, uint32_t bmax,
-                            bool tick, uint32_t extra = 0u) {
-  TileCtl* ctl = T.ctl;
-  atomicMax(&ctl->max_a[rec ^ 1u], amax);
-  atomicMax(&ctl->max_b[rec ^ 1u], bmax);
-  const uint32_t d = atomicAdd(&ctl->done, 1u);
-  if (d + 1u != T.items + extra) return;
-  volatile TileCtl* v = ctl;
+// The flip of a tile's control block once every item of its launch is done: slot `rec`'s largest
+// speeds cleared (every item has read them, its step's length), and for a tick the copy flipped
+// and the source's clock moved; a prime flips only the records. Run by the tile's last item
+// (finish_item) or by the resident tick's barrier.
+__device__ void flip_tile(const TileDesc& T, uint32_t rec, bool tick) {
+  volatile TileCtl* v = T.ctl;
   v->max_a[rec] = 0u;
   v->max_b[rec] = 0u;
   if (tick) {
@@ -223,6 +215,20 @@ __device__ void finish_item(const TileDesc& T, uint32_t rec, uint32_t amax, uint
   }
   v->rec = rec ^ 1u;
   v->done = 0u;
+}
+
+// The end of a work item (one thread): its largest speeds into slot rec ^ 1 of the tile's maxima
+// and, for the tile's last item, the flip. No fence: the item's planes, records and maxima are
+// read by the next launch, and the flip reads only fields no other item writes. `extra` counts a
+// CTA that folded the ledger apart from the items (1) or none (0).
+__device__ void finish_item(const TileDesc& T, uint32_t rec, uint32_t amax, uint32_t bmax,
+                            bool tick, uint32_t extra = 0u) {
+  TileCtl* ctl = T.ctl;
+  atomicMax(&ctl->max_a[rec ^ 1u], amax);
+  atomicMax(&ctl->max_b[rec ^ 1u], bmax);
+  const uint32_t d = atomicAdd(&ctl->done, 1u);
+  if (d + 1u != T.items + extra) return;
+  flip_tile(T, rec, tick);
 }
 
 // ---- the records ----------------------------------------------------------------------------
@@ -915,12 +921,269 @@ struct BlockSmem {
   uint32_t item, need, ab[4];
 };
 
+// The halo cell thread t reads (threads 0 .. 2 kBlkW + 2 kBlkH - 1; none for the others or past a
+// partial block's edge): its shared-memory slot, the cell it reads, and at the tile's edge the
+// ghost's sign for its normal velocity (slang:597-624).
+struct HaloCell {
+  float4* slot = nullptr;
+  int i = 0;
+  bool ghost = false, flip_v = false;
+  float sign = 1.0f;
+};
+
+__device__ __forceinline__ HaloCell halo_cell(BlockSmem& m, int t, int X0, int Y0, int rows,
+                                              int cols, int nx, int ny, uint32_t flags) {
+  HaloCell h;
+  if (t >= 2 * kBlkW + 2 * kBlkH) return h;
+  int gy, gx;
+  bool need;
+  if (t < kBlkW) {  // south row
+    const int c = t;
+    need = c < cols;
+    h.ghost = Y0 == 0;
+    gy = h.ghost ? Y0 : Y0 - 1;
+    gx = X0 + c;
+    h.sign = (flags & kFlagSouthOpen) ? 1.0f : -1.0f;
+    h.flip_v = true;
+    h.slot = &m.cell[0][c + 1];
+  } else if (t < 2 * kBlkW) {  // north row
+    const int c = t - kBlkW;
+    need = c < cols;
+    h.ghost = Y0 + rows >= ny;
+    gy = h.ghost ? Y0 + rows - 1 : Y0 + rows;
+    gx = X0 + c;
+    h.sign = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
+    h.flip_v = true;
+    h.slot = &m.cell[rows + 1][c + 1];
+  } else if (t < 2 * kBlkW + kBlkH) {  // west column
+    const int r = t - 2 * kBlkW;
+    need = r < rows;
+    h.ghost = X0 == 0;
+    gy = Y0 + r;
+    gx = h.ghost ? X0 : X0 - 1;
+    h.sign = (flags & kFlagWestOpen) ? 1.0f : -1.0f;
+    h.slot = &m.cell[r + 1][0];
+  } else {  // east column
+    const int r = t - 2 * kBlkW - kBlkH;
+    need = r < rows;
+    h.ghost = X0 + cols >= nx;
+    gy = Y0 + r;
+    gx = h.ghost ? X0 + cols - 1 : X0 + cols;
+    h.sign = (flags & kFlagEastOpen) ? 1.0f : -1.0f;
+    h.slot = &m.cell[r + 1][cols + 1];
+  }
+  h.i = gy * nx + gx;
+  if (!need) h.slot = nullptr;
+  return h;
+}
+
+// The tile's dt_main fold of the last update's records (slang:417-478) by the whole CTA, a thread
+// a virtual lane, into the ledger's next slot (`rec` is the slot the records are in).
+template <bool FIXED>
+__device__ __forceinline__ void fold_ledger(const TileDesc& T, BlockSmem& m, uint32_t rec,
+                                            float pa, float pb, float max_dt) {
+  const TileCtl* ctl = T.ctl;
+  fold_block(T.rec[rec], T.groups_x * T.groups_y, m.fold);
+  if (threadIdx.x == 0) {
+    LedgerBits l = ctl->ledger[rec];
+    ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
+                         T.cfl, T.cell_m, max_dt);
+    T.ctl->ledger[rec ^ 1u] = l;
+  }
+}
+
+// One 32 x 16 block of one tick: the three phases and the block's two records. `cur` is the copy
+// that holds the state, `rec` the record slot of the last update; pa and pb are the last update's
+// largest speeds. LATE_DT: `t_arg` is the ledger's time left, and the step's length is taken from
+// it once the block's loads are in flight (the resident tick, which knows its copy before it reads
+// the speeds); otherwise `t_arg` is the step's length. Whether the source applies and its scale
+// are the tick's. Warp 0's lane 0 leaves the block's largest speeds in ia, ib for the caller,
+// which counts the item. The tile's first block folds its ledger unless a CTA of its own does
+// (a.fold_apart).
+template <bool FIXED, bool MANNING, int THREADS, bool LATE_DT>
+__device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, const TileDesc& T,
+                                           uint32_t local, uint32_t cur, uint32_t rec, float pa,
+                                           float pb, float t_arg, bool apply, float scale,
+                                           uint32_t& ia, uint32_t& ib) {
+  constexpr int kBlkWarps = THREADS / 32;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+  const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
+  if (local == 0u && a.fold_apart == 0u) fold_ledger<FIXED>(T, m, rec, pa, pb, a.max_dt);
+  const int nx = int(T.nx), ny = int(T.ny);
+  const size_t n = size_t(T.nx) * T.ny;
+  const int rows = min(kBlkH, ny - Y0), cols = min(kBlkW, nx - X0);
+  const float* in = T.state[cur];
+  float* out = T.state[cur ^ 1u];
+  const float* bed = T.bed;
+  const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
+  const uint32_t flags = T.flags;
+  // The cells this thread updates: rows warp + kBlkWarps k of column t & 31.
+  constexpr int K = (kBlkH + kBlkWarps - 1) / kBlkWarps;
+  const int cc = lane;
+  // A thread of one cell (the 512-thread CTA) loads its bed and its halo cell with its state, so
+  // that the block waits on one round of loads; the 256-thread CTA loads them in phase 1 (its two
+  // cells' worth held from the start would spill).
+  constexpr bool kEarly = K == 1;
+  float rh[K], rhu[K], rhv[K], rz[K], rsrc[K];
+  bool live[K];
+  int gi[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int r = warp + kBlkWarps * k;
+    live[k] = r < rows && cc < cols;
+    gi[k] = (Y0 + r) * nx + X0 + cc;
+    rh[k] = rhu[k] = rhv[k] = rz[k] = rsrc[k] = 0.0f;
+    if (live[k]) {
+      rh[k] = in[gi[k]];
+      rhu[k] = in[n + gi[k]];
+      rhv[k] = in[2 * n + gi[k]];
+      if (kEarly) rz[k] = bed[gi[k]];
+      // A thread of one cell loads its source with its state, not after the barriers (two
+      // cells' worth would cost the 256-thread CTA spills).
+      if (K == 1 && apply) rsrc[k] = T.source[gi[k]];
+    }
+  }
+  HaloCell hc;
+  float qh = 0.0f, qhu = 0.0f, qhv = 0.0f, qz = 0.0f;
+  if (kEarly) {
+    hc = halo_cell(m, t, X0, Y0, rows, cols, nx, ny, flags);
+    if (hc.slot != nullptr) {
+      qh = in[hc.i];
+      qhu = in[n + hc.i];
+      qhv = in[2 * n + hc.i];
+      qz = bed[hc.i];
+    }
+  }
+  const float dt =
+      LATE_DT ? choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, t_arg) : t_arg;
+  uint32_t ga = 0u, gb = 0u;
+  bool opn_seen = false, rnd_seen = false;
+  if (!(dt > 0.0f)) {
+    // A step of no length: the state as it is, to the bit (slang:576-585).
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (live[k]) {
+        const int i = gi[k];
+        out[i] = rh[k];
+        out[n + i] = rhu[k];
+        out[2 * n + i] = rhv[k];
+        out[3 * n + i] = in[3 * n + i];
+        float ax, ay;
+        cell_speeds<FIXED>(g, dry, rh[k], rhu[k], rhv[k], ax, ay);
+        ga = max(ga, __float_as_uint(ax));
+        gb = max(gb, __float_as_uint(ay));
+      }
+    }
+  } else {
+    // 1. the cells and the halo ({h, z, u, v}; a ghost's normal velocity signed by its edge)
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (live[k])
+        m.cell[warp + kBlkWarps * k + 1][cc + 1] =
+            velocities<FIXED>(rh[k], rhu[k], rhv[k], kEarly ? rz[k] : bed[gi[k]], dry);
+    if (!kEarly) {
+      hc = halo_cell(m, t, X0, Y0, rows, cols, nx, ny, flags);
+      if (hc.slot != nullptr) {
+        qh = in[hc.i];
+        qhu = in[n + hc.i];
+        qhv = in[2 * n + hc.i];
+        qz = bed[hc.i];
+      }
+    }
+    if (hc.slot != nullptr) {
+      float4 v = velocities<FIXED>(qh, qhu, qhv, qz, dry);
+      if (hc.ghost) {
+        if (hc.flip_v) v.w = __fmul_rn(hc.sign, v.w);
+        else v.z = __fmul_rn(hc.sign, v.z);
+      }
+      *hc.slot = v;
+    }
+    __syncthreads();
+    // 2. the faces
+    const int nfx = rows * (cols + 1), nfy = (rows + 1) * cols;
+    const bool full = cols == kBlkW;
+    for (int q = t; q < nfx + nfy; q += THREADS) {
+      if (q < nfx) {
+        const int r = full ? q / (kBlkW + 1) : q / (cols + 1);
+        const int f = q - r * (cols + 1);
+        m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
+      } else {
+        const int q2 = q - nfx;
+        const int f = full ? q2 / kBlkW : q2 / cols;
+        const int c = q2 - f * cols;
+        m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
+      }
+    }
+    __syncthreads();
+    // 3. the updates
+    const float cell_m = T.cell_m;
+    const float area = __fmul_rn(cell_m, cell_m);
+    const float lam = Ops<FIXED>::div(dt, cell_m);
+    const float edge_volume = __fmul_rn(dt, cell_m);
+    const bool comp = (flags & kFlagCompensate) != 0u;
+    const bool manning = MANNING && (flags & kFlagManning) != 0u;
+    const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
+                       apply, comp, manning, (flags & 15u) != 0u};
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int r = warp + kBlkWarps * k;
+      if (r >= kBlkH) break;  // a warp past the block's rows (more than 512 threads)
+      float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
+      if (live[k]) {
+        const int i = gi[k];
+        float h, mu, mv, residual;
+        update_cell<FIXED>(uc, m.cell[r + 1][cc + 1], rhu[k], rhv[k],
+                           K == 1 ? rsrc[k] : (apply ? T.source[i] : 0.0f),
+                           comp ? in[3 * n + i] : 0.0f,
+                           manning ? T.manning[i] : 0.0f, m.fx[r][cc], m.fx[r][cc + 1],
+                           m.fy[r][cc], m.fy[r + 1][cc], X0 + cc, Y0 + r, h, mu, mv, residual,
+                           csrc, copn, crnd);
+        out[i] = h;
+        out[n + i] = mu;
+        out[2 * n + i] = mv;
+        if (comp) out[3 * n + i] = residual;
+        float ax, ay;
+        cell_speeds<FIXED>(g, dry, h, mu, mv, ax, ay);
+        ga = max(ga, __float_as_uint(ax));
+        gb = max(gb, __float_as_uint(ay));
+      }
+      const int slot = r * kStrip + cc;
+      m.ring[slot] = csrc;
+      m.ring[16 * kStrip + slot] = copn;
+      m.ring[32 * kStrip + slot] = crnd;
+      opn_seen |= copn != 0.0f;
+      rnd_seen |= crnd != 0.0f;
+    }
+  }
+  // The block's two groups: their largest speeds and the quantities some cell holds.
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) {
+    ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
+    gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
+  }
+  const bool any_opn = __any_sync(0xffffffffu, opn_seen);
+  const bool any_rnd = __any_sync(0xffffffffu, rnd_seen);
+  if ((lane & 15) == 0) {
+    atomicMax(&m.ab[(lane >> 4) * 2], ga);
+    atomicMax(&m.ab[(lane >> 4) * 2 + 1], gb);
+  }
+  if (lane == 0 && (any_opn || any_rnd))
+    atomicOr(&m.need, (any_opn ? 1u : 0u) | (any_rnd ? 2u : 0u));
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t need = m.need;
+    group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[lane < 16 ? 0 : 2],
+                  m.ab[lane < 16 ? 1 : 3], m.ring, dt > 0.0f && apply, (need & 1u) != 0u,
+                  (need & 2u) != 0u, ia, ib);
+  }
+}
+
 template <bool FIXED, bool MANNING, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(TickArgs a) {
   static_assert(THREADS >= int(kGroupCells) && THREADS % 32 == 0,
                 "fold_block takes a thread a virtual lane");
   static_assert(THREADS >= 2 * kBlkW + 2 * kBlkH, "a thread a halo cell");
-  constexpr int kBlkWarps = THREADS / 32;
   // The first item's tile descriptor into L1 while the grid before finishes: no tick or queue
   // slot writes a descriptor (only the host's uploads do, and a copy ends a dependent launch's
   // overlap), so it is the same before the wait as after it.
@@ -932,24 +1195,18 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
   if (a.go != nullptr && *a.go == 0u) return;
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int t = threadIdx.x;
   if (a.fold_apart != 0u && blockIdx.x + 1u == gridDim.x) {
-    // The tile's dt_main fold (slang:417-478) on a CTA of its own, beside the items: a single
-    // tile's launch of fewer items than SMs, whose item 0 would otherwise fold before it steps. It
-    // counts as one more item, so the flip waits for its read of slot `rec`.
+    // The tile's dt_main fold on a CTA of its own, beside the items: a single tile's launch of
+    // fewer items than SMs, whose item 0 would otherwise fold before it steps. It counts as one
+    // more item, so the flip waits for its read of slot `rec`.
     const TileDesc& T = a.tiles[0];
     const TileCtl* ctl = T.ctl;
     const uint32_t rec = ctl->rec;
     if (a.go != nullptr && !(ctl->ledger[rec].remaining_s > 0.0f)) return;  // a landed tile
     const float pa = __uint_as_float(ctl->max_a[rec]), pb = __uint_as_float(ctl->max_b[rec]);
-    fold_block(T.rec[rec], T.groups_x * T.groups_y, m.fold);
-    if (t == 0) {
-      LedgerBits l = ctl->ledger[rec];
-      ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
-                           T.cfl, T.cell_m, a.max_dt);
-      T.ctl->ledger[rec ^ 1u] = l;
-      finish_item(T, rec, 0u, 0u, true, 1u);
-    }
+    fold_ledger<FIXED>(T, m, rec, pa, pb, a.max_dt);
+    if (t == 0) finish_item(T, rec, 0u, 0u, true, 1u);
     return;
   }
   for (bool first = true;; first = false) {
@@ -964,7 +1221,6 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const uint32_t tile = item_tile_of(a.item_tile, item);
     const TileDesc& T = a.tiles[tile];
     const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
-    const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
     const TileCtl* ctl = T.ctl;
     const uint32_t cur = ctl->cur, rec = ctl->rec;
     const float pa = __uint_as_float(ctl->max_a[rec]), pb = __uint_as_float(ctl->max_b[rec]);
@@ -977,212 +1233,10 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const bool src_flag = (T.flags & kFlagSource) != 0u;
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
-    const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
-    if (local == 0u && a.fold_apart == 0u) {
-      // dt_main's fold of the last update's records (slang:417-478) by the whole CTA, a thread a
-      // virtual lane, into the ledger's next slot.
-      fold_block(T.rec[rec], T.groups_x * T.groups_y, m.fold);
-      if (t == 0) {
-        LedgerBits l = ctl->ledger[rec];
-        ledger_update<FIXED>(l, m.fold[0], m.fold[kGroupCells], m.fold[2 * kGroupCells], pa, pb,
-                             T.cfl, T.cell_m, a.max_dt);
-        T.ctl->ledger[rec ^ 1u] = l;
-      }
-    }
-    const int nx = int(T.nx), ny = int(T.ny);
-    const size_t n = size_t(T.nx) * T.ny;
-    const int rows = min(kBlkH, ny - Y0), cols = min(kBlkW, nx - X0);
-    const float* in = T.state[cur];
-    float* out = T.state[cur ^ 1u];
-    const float* bed = T.bed;
-    const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
-    const uint32_t flags = T.flags;
-    // The cells this thread updates: rows warp + kBlkWarps k of column t & 31.
-    constexpr int K = (kBlkH + kBlkWarps - 1) / kBlkWarps;
-    const int cc = lane;
-    float rh[K], rhu[K], rhv[K], rsrc[K];
-    bool live[K];
-    int gi[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int r = warp + kBlkWarps * k;
-      live[k] = r < rows && cc < cols;
-      gi[k] = (Y0 + r) * nx + X0 + cc;
-      rh[k] = rhu[k] = rhv[k] = rsrc[k] = 0.0f;
-      if (live[k]) {
-        rh[k] = in[gi[k]];
-        rhu[k] = in[n + gi[k]];
-        rhv[k] = in[2 * n + gi[k]];
-        // A thread of one cell loads its source with its state, not after the barriers (two
-        // cells' worth would cost the 256-thread CTA spills).
-        if (K == 1 && apply) rsrc[k] = T.source[gi[k]];
-      }
-    }
-    uint32_t ga = 0u, gb = 0u;
-    bool opn_seen = false, rnd_seen = false;
-    if (!(dt > 0.0f)) {
-      // A step of no length: the state as it is, to the bit (slang:576-585).
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        if (live[k]) {
-          const int i = gi[k];
-          out[i] = rh[k];
-          out[n + i] = rhu[k];
-          out[2 * n + i] = rhv[k];
-          out[3 * n + i] = in[3 * n + i];
-          float ax, ay;
-          cell_speeds<FIXED>(g, dry, rh[k], rhu[k], rhv[k], ax, ay);
-          ga = max(ga, __float_as_uint(ax));
-          gb = max(gb, __float_as_uint(ay));
-        }
-      }
-    } else {
-      const float sw = (flags & kFlagWestOpen) ? 1.0f : -1.0f;
-      const float se = (flags & kFlagEastOpen) ? 1.0f : -1.0f;
-      const float ss = (flags & kFlagSouthOpen) ? 1.0f : -1.0f;
-      const float sn = (flags & kFlagNorthOpen) ? 1.0f : -1.0f;
-      // 1. the cells and the halo
-#pragma unroll
-      for (int k = 0; k < K; ++k)
-        if (live[k])
-          m.cell[warp + kBlkWarps * k + 1][cc + 1] =
-              velocities<FIXED>(rh[k], rhu[k], rhv[k], bed[gi[k]], dry);
-      if (t < 2 * kBlkW + 2 * kBlkH) {
-        int r, c, gy, gx;  // the halo cell's local place and the global cell it reads
-        float4* slot;
-        bool ghost;
-        float sign = 1.0f;
-        bool flip_v = false;
-        bool need;
-        if (t < kBlkW) {  // south row
-          c = t;
-          r = -1;
-          need = c < cols;
-          ghost = Y0 == 0;
-          gy = ghost ? Y0 : Y0 - 1;
-          gx = X0 + c;
-          sign = ss;
-          flip_v = true;
-          slot = &m.cell[0][c + 1];
-        } else if (t < 2 * kBlkW) {  // north row
-          c = t - kBlkW;
-          r = rows;
-          need = c < cols;
-          ghost = Y0 + rows >= ny;
-          gy = ghost ? Y0 + rows - 1 : Y0 + rows;
-          gx = X0 + c;
-          sign = sn;
-          flip_v = true;
-          slot = &m.cell[rows + 1][c + 1];
-        } else if (t < 2 * kBlkW + kBlkH) {  // west column
-          r = t - 2 * kBlkW;
-          c = -1;
-          need = r < rows;
-          ghost = X0 == 0;
-          gy = Y0 + r;
-          gx = ghost ? X0 : X0 - 1;
-          sign = sw;
-          slot = &m.cell[r + 1][0];
-        } else {  // east column
-          r = t - 2 * kBlkW - kBlkH;
-          c = cols;
-          need = r < rows;
-          ghost = X0 + cols >= nx;
-          gy = Y0 + r;
-          gx = ghost ? X0 + cols - 1 : X0 + cols;
-          sign = se;
-          slot = &m.cell[r + 1][cols + 1];
-        }
-        if (need) {
-          const int i = gy * nx + gx;
-          float4 v = load_cell<FIXED>(in, in + n, in + 2 * n, bed, i, dry);
-          if (ghost) {
-            if (flip_v) v.w = __fmul_rn(sign, v.w);
-            else v.z = __fmul_rn(sign, v.z);
-          }
-          *slot = v;
-        }
-      }
-      __syncthreads();
-      // 2. the faces
-      const int nfx = rows * (cols + 1), nfy = (rows + 1) * cols;
-      const bool full = cols == kBlkW;
-      for (int q = t; q < nfx + nfy; q += THREADS) {
-        if (q < nfx) {
-          const int r = full ? q / (kBlkW + 1) : q / (cols + 1);
-          const int f = q - r * (cols + 1);
-          m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
-        } else {
-          const int q2 = q - nfx;
-          const int f = full ? q2 / kBlkW : q2 / cols;
-          const int c = q2 - f * cols;
-          m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
-        }
-      }
-      __syncthreads();
-      // 3. the updates
-      const float cell_m = T.cell_m;
-      const float area = __fmul_rn(cell_m, cell_m);
-      const float lam = Ops<FIXED>::div(dt, cell_m);
-      const float edge_volume = __fmul_rn(dt, cell_m);
-      const bool comp = (flags & kFlagCompensate) != 0u;
-      const bool manning = MANNING && (flags & kFlagManning) != 0u;
-      const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
-                         apply, comp, manning, (flags & 15u) != 0u};
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        const int r = warp + kBlkWarps * k;
-        if (r >= kBlkH) break;  // a warp past the block's rows (more than 512 threads)
-        float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
-        if (live[k]) {
-          const int i = gi[k];
-          float h, mu, mv, residual;
-          update_cell<FIXED>(uc, m.cell[r + 1][cc + 1], rhu[k], rhv[k],
-                             K == 1 ? rsrc[k] : (apply ? T.source[i] : 0.0f),
-                             comp ? in[3 * n + i] : 0.0f,
-                             manning ? T.manning[i] : 0.0f, m.fx[r][cc], m.fx[r][cc + 1],
-                             m.fy[r][cc], m.fy[r + 1][cc], X0 + cc, Y0 + r, h, mu, mv, residual,
-                             csrc, copn, crnd);
-          out[i] = h;
-          out[n + i] = mu;
-          out[2 * n + i] = mv;
-          if (comp) out[3 * n + i] = residual;
-          float ax, ay;
-          cell_speeds<FIXED>(g, dry, h, mu, mv, ax, ay);
-          ga = max(ga, __float_as_uint(ax));
-          gb = max(gb, __float_as_uint(ay));
-        }
-        const int slot = r * kStrip + cc;
-        m.ring[slot] = csrc;
-        m.ring[16 * kStrip + slot] = copn;
-        m.ring[32 * kStrip + slot] = crnd;
-        opn_seen |= copn != 0.0f;
-        rnd_seen |= crnd != 0.0f;
-      }
-    }
-    // The block's two groups: their largest speeds and the quantities some cell holds.
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) {
-      ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
-      gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
-    }
-    const bool any_opn = __any_sync(0xffffffffu, opn_seen);
-    const bool any_rnd = __any_sync(0xffffffffu, rnd_seen);
-    if ((lane & 15) == 0) {
-      atomicMax(&m.ab[(lane >> 4) * 2], ga);
-      atomicMax(&m.ab[(lane >> 4) * 2 + 1], gb);
-    }
-    if (lane == 0 && (any_opn || any_rnd))
-      atomicOr(&m.need, (any_opn ? 1u : 0u) | (any_rnd ? 2u : 0u));
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t ia = 0u, ib = 0u;
-      const uint32_t need = m.need;
-      group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[lane < 16 ? 0 : 2],
-                    m.ab[lane < 16 ? 1 : 3], m.ring, dt > 0.0f && apply, (need & 1u) != 0u,
-                    (need & 2u) != 0u, ia, ib);
-      if (lane == 0) finish_item(T, rec, ia, ib, true, a.fold_apart);
-    }
+    uint32_t ia = 0u, ib = 0u;
+    block_item<FIXED, MANNING, THREADS, false>(a, m, T, local, cur, rec, pa, pb, dt, apply, scale,
+                                               ia, ib);
+    if (t == 0) finish_item(T, rec, ia, ib, true, a.fold_apart);
     __syncthreads();
   }
   if (t == 0 && gridDim.x < a.n_items) {  // the counter was read
@@ -1193,6 +1247,143 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
       __threadfence();
     }
   }
+}
+
+// ---- the resident tick: many ticks of one small tile in one launch ----------------------------
+//
+// A tile of no more blocks than the device holds CTAs of the wide block tick (the 256 x 256 tile's
+// 128) steps `ticks` ticks in one cooperative launch: a CTA a block for the whole launch, one CTA
+// more for the ledger's fold, and a grid barrier between ticks in place of the launch boundary.
+// Each tick is the block tick's own (block_item, fold_ledger: the same arithmetic, records and
+// ledger). What the launches' flips would do tick by tick is kept in registers (the copy and the
+// record slot follow the ticks' parity, the source's clock its count) and the largest speeds in
+// three rotating slots of the ResidentCtl (tick k reads slot k % 3, adds to slot (k + 1) % 3, and
+// the fold's CTA clears slot (k + 2) % 3, read at tick k - 1); after the last tick CTA 0 writes the
+// control block as the last launch's flip would have left it.
+//
+// The barrier: each CTA's thread 0 adds one to `arrived` with release semantics and polls it
+// with acquire semantics until it reaches the tick's count (the host zeroes it before a launch).
+// A wait is bounded: past kResidentWaitNs it marks the error word and the CTA leaves, and so
+// does every CTA that then sees the mark, so the launch ends; the host reads the word.
+constexpr uint64_t kResidentWaitNs = 1000000000ull;  // a second
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Returns false where the wait gave up.
+__device__ __forceinline__ bool resident_barrier(ResidentCtl* rc, uint32_t target) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&rc->arrived) : "memory");
+    int ok = 1;
+    const uint64_t t0 = global_ns();
+    for (uint32_t polls = 1;; ++polls) {
+      uint32_t c;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&rc->arrived) : "memory");
+      if (c >= target) break;
+      if ((polls & 63u) == 0u) {
+        const uint32_t e = static_cast<const volatile ResidentCtl*>(rc)->error;
+        if (e != 0u || global_ns() - t0 > kResidentWaitNs) {
+          atomicOr(&rc->error, 1u);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <bool FIXED, bool MANNING>
+__global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickArgs a,
+                                                                          uint32_t ticks,
+                                                                          ResidentCtl* rc) {
+  extern __shared__ float4 smem_raw[];
+  BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
+  const int t = threadIdx.x;
+  const TileDesc& T = a.tiles[0];
+  TileCtl* ctl = T.ctl;
+  const uint32_t cur0 = ctl->cur, rec0 = ctl->rec, ticks0 = ctl->ticks;
+  uint32_t cur = cur0, rec = rec0, phase = ctl->src_phase;
+  const bool src_flag = (T.flags & kFlagSource) != 0u;
+  const uint32_t every = T.source_every;
+  const float scale = every > 1u ? float(every) : 1.0f;
+  const bool folder = blockIdx.x == a.n_items;
+  const uint32_t n = gridDim.x;
+  uint32_t slot = 0u;  // k % 3
+  for (uint32_t k = 0; k < ticks; ++k) {
+    // What the last tick left: the control block's at the first tick, the rotating slot after.
+    uint32_t ua, ub;
+    float remaining;
+    if (k == 0u) {
+      ua = ctl->max_a[rec0];
+      ub = ctl->max_b[rec0];
+      remaining = ctl->ledger[rec0].remaining_s;
+    } else {
+      uint4 w;
+      asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                   : "=r"(w.x), "=r"(w.y), "=r"(w.z), "=r"(w.w)
+                   : "l"(&rc->slot[slot]));
+      ua = w.x;
+      ub = w.y;
+      remaining = __uint_as_float(w.z);
+    }
+    const float pa = __uint_as_float(ua), pb = __uint_as_float(ub);
+    const uint32_t next = slot == 2u ? 0u : slot + 1u, spare = next == 2u ? 0u : next + 1u;
+    if (folder) {
+      fold_ledger<FIXED>(T, m, rec, pa, pb, a.max_dt);
+      if (t == 0) {
+        // The new ledger (thread 0 wrote it) gives the next tick its time left.
+        rc->slot[next].remaining_s = static_cast<const volatile TileCtl*>(ctl)->ledger[rec ^ 1u].remaining_s;
+        rc->slot[spare].max_a = 0u;
+        rc->slot[spare].max_b = 0u;
+      }
+    } else {
+      // m.need and m.ab were last read before the last barrier; block_item's first barrier orders
+      // these writes before their use.
+      if (t == 0) m.need = 0u;
+      if (t < 4) m.ab[t] = 0u;
+      const bool apply = src_flag && (every <= 1u || phase + 1u == every);
+      uint32_t ia = 0u, ib = 0u;
+      block_item<FIXED, MANNING, kBlkWideThreads, true>(a, m, T, blockIdx.x, cur, rec, pa, pb,
+                                                        remaining, apply, scale, ia, ib);
+      if (t == 0) {
+        atomicMax(&rc->slot[next].max_a, ia);
+        atomicMax(&rc->slot[next].max_b, ib);
+      }
+    }
+    if (!resident_barrier(rc, n * (k + 1u))) return;
+    if (src_flag && every > 1u) phase = phase + 1u == every ? 0u : phase + 1u;
+    cur ^= 1u;
+    rec ^= 1u;
+    slot = next;
+  }
+  if (blockIdx.x == 0 && t == 0 && ticks > 0u) {
+    // Every CTA is past the last barrier and none reads the control block again.
+    volatile TileCtl* w = ctl;
+    const volatile ResidentCtl* vr = rc;
+    w->max_a[rec] = vr->slot[slot].max_a;
+    w->max_b[rec] = vr->slot[slot].max_b;
+    w->max_a[rec ^ 1u] = 0u;
+    w->max_b[rec ^ 1u] = 0u;
+    w->cur = cur;
+    w->rec = rec;
+    w->src_phase = phase;
+    w->ticks = ticks0 + ticks;
+  }
+}
+
+// A check of the barrier's bounded wait alone: `n` CTAs of which the last never arrives, so the
+// others give up after the bound and mark the error word. The host zeroes `rc` and reads it.
+__global__ void resident_barrier_probe_kernel(ResidentCtl* rc, uint32_t n) {
+  if (blockIdx.x + 1u == gridDim.x) return;  // the CTA that does not arrive
+  resident_barrier(rc, n);
 }
 
 // The records of a state written from the host (prime_main, slang:373-386): a warp an item. The
@@ -1602,6 +1793,66 @@ cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain,
     case BlockShape::k32x16w: return block_launch<kBlkWideThreads>(fixed, manning, a, grid, s);
   }
   return cudaErrorInvalidValue;
+}
+
+namespace {
+const void* resident_fn(bool fixed, bool manning) {
+  if (fixed)
+    return manning ? (const void*)tick_resident_kernel<true, true>
+                   : (const void*)tick_resident_kernel<true, false>;
+  return manning ? (const void*)tick_resident_kernel<false, true>
+                 : (const void*)tick_resident_kernel<false, false>;
+}
+}  // namespace
+
+int resident_capacity(bool fixed, bool manning) {
+  const void* fn = resident_fn(fixed, manning);
+  const int smem = int(sizeof(BlockSmem));
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return 0;
+  int blocks = 0, device = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kBlkWideThreads, smem) !=
+          cudaSuccess ||
+      cudaGetDevice(&device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return 0;
+  return blocks * sms;
+}
+
+cudaError_t launch_tick_resident(bool fixed, bool manning, const TickArgs& args, uint32_t ticks,
+                                 ResidentCtl* rc, cudaStream_t s) {
+  TickArgs a = args;
+  a.n_whole = a.n_items;
+  a.fold_apart = 1u;
+  if (cudaMemsetAsync(rc, 0, sizeof(ResidentCtl), s) != cudaSuccess) return cudaGetLastError();
+  void (*k)(TickArgs, uint32_t, ResidentCtl*) =
+      fixed ? (manning ? tick_resident_kernel<true, true> : tick_resident_kernel<true, false>)
+            : (manning ? tick_resident_kernel<false, true> : tick_resident_kernel<false, false>);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.n_items + 1u);
+  cfg.blockDim = dim3(kBlkWideThreads);
+  cfg.dynamicSmemBytes = sizeof(BlockSmem);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, a, ticks, rc);
+}
+
+cudaError_t launch_barrier_probe(ResidentCtl* rc, uint32_t n, cudaStream_t s) {
+  if (cudaMemsetAsync(rc, 0, sizeof(ResidentCtl), s) != cudaSuccess) return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n);
+  cfg.blockDim = dim3(32);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, resident_barrier_probe_kernel, rc, n);
 }
 
 cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaStream_t s) {

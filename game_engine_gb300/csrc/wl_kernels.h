@@ -9,6 +9,7 @@ namespace wlc {
 
 struct TileDesc;
 struct WorkCtl;
+struct ResidentCtl;
 
 // A tick launch: the tiles, which tile each work item belongs to (null: all items of tile 0), the
 // launch's work counter and the step's max_dt. `go`, when not null, is a device word read at the
@@ -49,6 +50,17 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning, bool plain);
 cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain, const TickArgs& a,
                         int grid, cudaStream_t s);
 // The records of the states just written (one CTA a work item, the same items as the tick's).
+// The resident tick: `ticks` ticks of tile 0 (the wide block tick's items) in one cooperative
+// launch of a.n_items + 1 CTAs, a grid barrier between ticks. `rc` (zeroed here, on `s`, before
+// the launch) holds the barrier's words; a nonzero error word after the launch means a wait gave
+// up and the state is not the ticks' result.
+cudaError_t launch_tick_resident(bool fixed, bool manning, const TickArgs& a, uint32_t ticks,
+                                 ResidentCtl* rc, cudaStream_t s);
+// The resident tick's CTAs the current device holds at once (0 on an error).
+int resident_capacity(bool fixed, bool manning);
+// The barrier's bounded wait alone: n CTAs, the last of which never arrives; the others give up
+// after a second and set rc's error word (rc is zeroed here first).
+cudaError_t launch_barrier_probe(ResidentCtl* rc, uint32_t n, cudaStream_t s);
 cudaError_t launch_prime(BlockShape shape, bool fixed, const TickArgs& a, cudaStream_t s);
 cudaError_t launch_length_pass(bool fixed, const TileDesc* tiles, uint32_t tile, float max_dt,
                                cudaStream_t s);

@@ -161,9 +161,12 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   const size_t off_first = total;
   total += align_up(nt * sizeof(uint64_t));
   // The work counters: one for launches over the whole set, one per tile for its own launches
-  // (tiles launched alone may run concurrently on different streams).
+  // (tiles launched alone may run concurrently on different streams), then the resident tick's
+  // words.
   const size_t off_work = total;
   total += align_up((1 + nt) * sizeof(WorkCtl));
+  const size_t off_res = total;
+  total += align_up(sizeof(ResidentCtl));
   if (!check(cudaMalloc(&base_, total), err, "cudaMalloc")) {
     base_ = nullptr;
     destroy();
@@ -178,6 +181,7 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   d_desc_ = reinterpret_cast<TileDesc*>(base_ + off_desc);
   d_first_ = reinterpret_cast<uint64_t*>(base_ + off_first);
   d_work_ = reinterpret_cast<WorkCtl*>(base_ + off_work);
+  d_res_ = reinterpret_cast<ResidentCtl*>(base_ + off_res);
   if (!check(cudaMemcpyAsync(d_first_, first_.data(), nt * sizeof(uint64_t),
                              cudaMemcpyHostToDevice, stream_),
              err, "upload of the cell offsets")) {
@@ -236,6 +240,9 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
         destroy();
         return false;
       }
+  // The resident tick's capacity, taken here rather than at a launch that may be under capture.
+  resident_cap_[0] = resident_capacity(fixed_, false);
+  resident_cap_[1] = resident_capacity(fixed_, true);
   if (!layout_items(shape, order, err)) {
     destroy();
     return false;
@@ -340,10 +347,18 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   if (wide && d_item_tile_ == nullptr) {
     a.fold_apart = 1u;
     grid = int(n_items_) + 1;
+    if (go == nullptr && count > 1) {
+      if (grid <= resident_cap_[manning ? 1 : 0]) {
+        resident_used_ = true;
+        ++tick_launches_;
+        return launch_tick_resident(fixed_, manning, a, count, d_res_, s);
+      }
+    }
   }
   for (uint32_t i = 0; i < count; ++i) {
     const cudaError_t e = launch_tick(shape, fixed_, manning, plain_set, a, grid, s);
     if (e != cudaSuccess) return e;
+    ++tick_launches_;
   }
   return cudaSuccess;
 }
@@ -401,7 +416,21 @@ bool TileSet::wait(std::string* err) {
     if (err) *err = "water_live: the device did not finish within the wait limit";
     return false;
   }
-  return check(e, err, "the device");
+  if (!check(e, err, "the device")) return false;
+  if (resident_used_) {
+    // A resident launch's barrier marks its error word where a wait gave up; the state is then
+    // not the ticks' result.
+    resident_used_ = false;
+    uint32_t word = 0u;
+    if (!check(cudaMemcpy(&word, &d_res_->error, sizeof word, cudaMemcpyDeviceToHost), err,
+               "read-back of the resident tick's barrier"))
+      return false;
+    if (word != 0u) {
+      if (err) *err = "water_live: the resident tick's grid barrier gave up (a CTA did not arrive)";
+      return false;
+    }
+  }
+  return true;
 }
 
 bool TileSet::prime(std::string* err) {

@@ -39,9 +39,13 @@ class TileSet {
   bool reshape(BlockShape shape, const std::vector<uint32_t>& order, std::string* err);
 
   // ---- asynchronous, on `s` -----------------------------------------------------------------
-  // `go`: a tick queue's word that lets the launches step (null: always).
+  // `go`: a tick queue's word that lets the launches step (null: always). A single tile of no
+  // more blocks than the device holds resident CTAs steps two or more ticks in one cooperative
+  // launch (the resident tick); otherwise a launch a tick.
   cudaError_t enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
                             const uint32_t* go = nullptr);
+  // Tick kernel launches enqueued since create (a diagnosis counter).
+  uint64_t tick_launches() const { return tick_launches_; }
   // One tile's own tick (the per-tile-launch form): only that tile's work items.
   cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);
   cudaError_t enqueue_prime(cudaStream_t s);
@@ -122,6 +126,10 @@ class TileSet {
   TileDesc* d_desc_ = nullptr;
   TileCtl* d_ctl_ = nullptr;
   WorkCtl* d_work_ = nullptr;
+  ResidentCtl* d_res_ = nullptr;  // the resident tick's barrier words and largest speeds
+  int resident_cap_[2] = {0, 0};  // resident CTAs the device holds (without, with Manning's)
+  bool resident_used_ = false;      // a resident launch since the last wait()
+  uint64_t tick_launches_ = 0;
   uint32_t* d_item_tile_ = nullptr;  // the tile of each work item (null for one tile)
   uint32_t n_items_ = 0;
   int grid_ = 0;

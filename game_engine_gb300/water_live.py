@@ -204,6 +204,11 @@ class DeviceStep:
             return False
         return True
 
+    def tick_launches(self) -> int:
+        """Tick kernel launches enqueued since create (a diagnosis counter): a small tile steps a
+        call's ticks in one resident launch, a larger one a launch a tick."""
+        return int(lib().wl_tick_launches(self._h)) if self._h is not None else 0
+
     def run_steps(self, count: int, max_dt: float) -> bool:
         return self._ok(lib().wl_run_steps(self._h, int(count), float(max_dt), self._buf,
                                            len(self._buf)))

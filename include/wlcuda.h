@@ -122,6 +122,10 @@ int wl_valid(const wl_step* step);
 /* DeviceStep::cell_count / group_count (water_live.h:174-175); 0 for an invalid handle. */
 uint32_t wl_cell_count(const wl_step* step);
 uint32_t wl_group_count(const wl_step* step);
+/* Tick kernel launches enqueued since create (no counterpart in the reference: a diagnosis
+ * counter). A tile of no more 32 x 16 blocks than the device holds resident CTAs steps a call's two
+ * or more ticks in one launch; other tiles take a launch a tick. 0 for an invalid handle. */
+uint64_t wl_tick_launches(const wl_step* step);
 
 /* DeviceStep::write_state (water_live.cpp:271-314): each array n = nx * ny doubles, rounded to
  * float; plane 3 zeroed; the ledger emptied; the source clock restarted. */
@@ -178,6 +182,12 @@ int wl_run_length_pass(wl_step* step, float max_dt, char* err, size_t err_len);
 
 /* water_live::hash_floats (water_live.cpp:90-101). */
 uint64_t wl_hash_floats(const float* values, size_t count);
+
+/* A check of the resident tick's grid barrier (no counterpart in the reference): `ctas` CTAs
+ * (2 or more) meet at the barrier on `device` except the last, which never arrives, so the others'
+ * bounded wait runs out (about a second) and marks the barrier's error word. WL_OK when every CTA
+ * left and the word was marked; WL_ERR_CUDA otherwise. */
+int wl_resident_barrier_check(int device, uint32_t ctas, char* err, size_t err_len);
 
 /* The step's own stream (a cudaStream_t), for callers that order work against it. */
 wl_stream wl_step_stream(wl_step* step);
