@@ -994,16 +994,13 @@ __device__ __forceinline__ void fold_ledger(const TileDesc& T, BlockSmem& m, uin
 
 // One 32 x 16 block of one tick: the three phases and the block's two records. `cur` is the copy
 // that holds the state, `rec` the record slot of the last update; pa and pb are the last update's
-// largest speeds. LATE_DT: `t_arg` is the ledger's time left, and the step's length is taken from
-// it once the block's loads are in flight (the resident tick, which knows its copy before it reads
-// the speeds); otherwise `t_arg` is the step's length. Whether the source applies and its scale
-// are the tick's. Warp 0's lane 0 leaves the block's largest speeds in ia, ib for the caller,
-// which counts the item. The tile's first block folds its ledger unless a CTA of its own does
-// (a.fold_apart).
-template <bool FIXED, bool MANNING, int THREADS, bool LATE_DT>
+// largest speeds; dt, whether the source applies and its scale are the tick's. Warp 0's lane 0
+// leaves the block's largest speeds in ia, ib for the caller, which counts the item. The tile's
+// first block folds its ledger unless a CTA of its own does (a.fold_apart).
+template <bool FIXED, bool MANNING, int THREADS>
 __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, const TileDesc& T,
                                            uint32_t local, uint32_t cur, uint32_t rec, float pa,
-                                           float pb, float t_arg, bool apply, float scale,
+                                           float pb, float dt, bool apply, float scale,
                                            uint32_t& ia, uint32_t& ib) {
   constexpr int kBlkWarps = THREADS / 32;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -1055,8 +1052,6 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
       qz = bed[hc.i];
     }
   }
-  const float dt =
-      LATE_DT ? choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, t_arg) : t_arg;
   uint32_t ga = 0u, gb = 0u;
   bool opn_seen = false, rnd_seen = false;
   if (!(dt > 0.0f)) {
@@ -1234,8 +1229,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
     uint32_t ia = 0u, ib = 0u;
-    block_item<FIXED, MANNING, THREADS, false>(a, m, T, local, cur, rec, pa, pb, dt, apply, scale,
-                                               ia, ib);
+    block_item<FIXED, MANNING, THREADS>(a, m, T, local, cur, rec, pa, pb, dt, apply, scale, ia,
+                                        ib);
     if (t == 0) finish_item(T, rec, ia, ib, true, a.fold_apart);
     __syncthreads();
   }
@@ -1273,12 +1268,18 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Returns false where the wait gave up.
-__device__ __forceinline__ bool resident_barrier(ResidentCtl* rc, uint32_t target) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
+// The barrier in two halves, so that a CTA works while it waits: `resident_arrive` (after a CTA
+// barrier: every thread's writes of the tick are done) adds the CTA's arrival with release
+// semantics; `resident_wait` polls with acquire semantics until `target` CTAs have arrived, then
+// meets the CTA's threads. Returns false where the wait gave up.
+__device__ __forceinline__ void resident_arrive(ResidentCtl* rc) {
+  if (threadIdx.x == 0)
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&rc->arrived) : "memory");
+}
+
+__device__ __forceinline__ bool resident_wait(ResidentCtl* rc, uint32_t target) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
     int ok = 1;
     const uint64_t t0 = global_ns();
     for (uint32_t polls = 1;; ++polls) {
@@ -1300,22 +1301,94 @@ __device__ __forceinline__ bool resident_barrier(ResidentCtl* rc, uint32_t targe
   return s_ok != 0;
 }
 
+__device__ __forceinline__ bool resident_barrier(ResidentCtl* rc, uint32_t target) {
+  __syncthreads();
+  resident_arrive(rc);
+  return resident_wait(rc, target);
+}
+
+// The faces of a 32 x 16 block whose cells are all the block's own (none on the halo): x faces
+// 1 .. cols - 1 of each row and y faces 1 .. rows - 1 of each column. A CTA computes the next
+// tick's while it waits at the barrier; the boundary faces need the halo, read after it.
+template <bool FIXED, int THREADS>
+__device__ __forceinline__ void interior_faces(BlockSmem& m, int rows, int cols, float g,
+                                               float hg) {
+  const int nfx = rows * (cols - 1), nfy = (rows - 1) * cols;
+  for (int q = threadIdx.x; q < nfx + nfy; q += THREADS) {
+    if (q < nfx) {
+      const int r = q / (cols - 1), f = q - r * (cols - 1) + 1;
+      m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
+    } else {
+      const int q2 = q - nfx;
+      const int f = q2 / cols + 1, c = q2 - (f - 1) * cols;
+      m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
+    }
+  }
+}
+
+// The faces on the block's boundary (x faces 0 and cols, y faces 0 and rows), once the halo is in.
+template <bool FIXED>
+__device__ __forceinline__ void boundary_faces(BlockSmem& m, int rows, int cols, float g,
+                                               float hg) {
+  const int q = threadIdx.x;
+  if (q < 2 * rows) {
+    const int r = q >> 1, f = (q & 1) ? cols : 0;
+    m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
+  } else if (q < 2 * rows + 2 * cols) {
+    const int q2 = q - 2 * rows;
+    const int c = q2 >> 1, f = (q2 & 1) ? rows : 0;
+    m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
+  }
+}
+
 template <bool FIXED, bool MANNING>
 __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickArgs a,
                                                                           uint32_t ticks,
                                                                           ResidentCtl* rc) {
+  static_assert(kBlkWideThreads == kBlkW * kBlkH, "a thread a cell");
+  static_assert(kBlkWideThreads >= 2 * kBlkW + 2 * kBlkH, "a thread a boundary face");
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const TileDesc& T = a.tiles[0];
   TileCtl* ctl = T.ctl;
   const uint32_t cur0 = ctl->cur, rec0 = ctl->rec, ticks0 = ctl->ticks;
   uint32_t cur = cur0, rec = rec0, phase = ctl->src_phase;
-  const bool src_flag = (T.flags & kFlagSource) != 0u;
+  const uint32_t flags = T.flags;
+  const bool src_flag = (flags & kFlagSource) != 0u;
   const uint32_t every = T.source_every;
   const float scale = every > 1u ? float(every) : 1.0f;
   const bool folder = blockIdx.x == a.n_items;
   const uint32_t n = gridDim.x;
+  // The block and this thread's cell (row `warp`, column `lane`), held across the ticks: its
+  // state in registers, its {h, z, u, v} in the shared cell array.
+  const uint32_t local = folder ? 0u : blockIdx.x;
+  const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+  const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
+  const int nx = int(T.nx), ny = int(T.ny);
+  const size_t nn = size_t(T.nx) * T.ny;
+  const int rows = min(kBlkH, ny - Y0), cols = min(kBlkW, nx - X0);
+  const bool live = !folder && warp < rows && lane < cols;
+  const int gi = (Y0 + warp) * nx + X0 + lane;
+  const float g = T.gravity, dry = T.dry, hg = __fmul_rn(0.5f, g);
+  const bool comp = (flags & kFlagCompensate) != 0u;
+  const bool manning = MANNING && (flags & kFlagManning) != 0u;
+  const float cell_m = T.cell_m;
+  const float area = __fmul_rn(cell_m, cell_m);
+  float h = 0.0f, hu = 0.0f, hv = 0.0f, z = 0.0f, src = 0.0f, resid = 0.0f, mn = 0.0f;
+  if (live) {
+    const float* in = T.state[cur0];
+    h = in[gi];
+    hu = in[nn + gi];
+    hv = in[2 * nn + gi];
+    resid = comp ? in[3 * nn + gi] : 0.0f;
+    z = T.bed[gi];
+    if (src_flag) src = T.source[gi];
+    if (manning) mn = T.manning[gi];
+    m.cell[warp + 1][lane + 1] = velocities<FIXED>(h, hu, hv, z, dry);
+  }
+  __syncthreads();
+  if (!folder) interior_faces<FIXED, kBlkWideThreads>(m, rows, cols, g, hg);
   uint32_t slot = 0u;  // k % 3
   for (uint32_t k = 0; k < ticks; ++k) {
     // What the last tick left: the control block's at the first tick, the rotating slot after.
@@ -1340,25 +1413,112 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
       fold_ledger<FIXED>(T, m, rec, pa, pb, a.max_dt);
       if (t == 0) {
         // The new ledger (thread 0 wrote it) gives the next tick its time left.
-        rc->slot[next].remaining_s = static_cast<const volatile TileCtl*>(ctl)->ledger[rec ^ 1u].remaining_s;
+        rc->slot[next].remaining_s =
+            static_cast<const volatile TileCtl*>(ctl)->ledger[rec ^ 1u].remaining_s;
         rc->slot[spare].max_a = 0u;
         rc->slot[spare].max_b = 0u;
       }
+      __syncthreads();
+      resident_arrive(rc);
     } else {
-      // m.need and m.ab were last read before the last barrier; block_item's first barrier orders
-      // these writes before their use.
+      // m.need and m.ab were last read before the last barrier; the barriers below order these
+      // writes before their use.
       if (t == 0) m.need = 0u;
       if (t < 4) m.ab[t] = 0u;
-      const bool apply = src_flag && (every <= 1u || phase + 1u == every);
-      uint32_t ia = 0u, ib = 0u;
-      block_item<FIXED, MANNING, kBlkWideThreads, true>(a, m, T, blockIdx.x, cur, rec, pa, pb,
-                                                        remaining, apply, scale, ia, ib);
-      if (t == 0) {
-        atomicMax(&rc->slot[next].max_a, ia);
-        atomicMax(&rc->slot[next].max_b, ib);
+      const float* in = T.state[cur];
+      float* out = T.state[cur ^ 1u];
+      // 1. the halo (the neighbours' last tick, or a ghost of this block's own edge)
+      const HaloCell hc = halo_cell(m, t, X0, Y0, rows, cols, nx, ny, flags);
+      if (hc.slot != nullptr) {
+        float4 v = velocities<FIXED>(in[hc.i], in[nn + hc.i], in[2 * nn + hc.i], T.bed[hc.i], dry);
+        if (hc.ghost) {
+          if (hc.flip_v) v.w = __fmul_rn(hc.sign, v.w);
+          else v.z = __fmul_rn(hc.sign, v.z);
+        }
+        *hc.slot = v;
       }
+      const float dt = choose_dt<FIXED>(pa, pb, T.cfl, cell_m, a.max_dt, remaining);
+      const bool apply = src_flag && (every <= 1u || phase + 1u == every);
+      __syncthreads();
+      // 2. the boundary faces (the interior ones were taken while waiting at the last barrier)
+      if (dt > 0.0f) boundary_faces<FIXED>(m, rows, cols, g, hg);
+      __syncthreads();
+      // 3. the update, its speeds, and the next tick's velocities
+      uint32_t ga = 0u, gb = 0u;
+      bool opn_seen = false, rnd_seen = false;
+      float csrc = 0.0f, copn = 0.0f, crnd = 0.0f;
+      if (live) {
+        // Plane 3 (the compensated source's remainder): carried in `resid` where compensating
+        // (each tick writes it); otherwise a tick leaves the output copy's as it was and a step of
+        // no length copies the input copy's.
+        float h2 = h, mu = hu, mv = hv, residual = resid;
+        if (dt > 0.0f) {
+          const float lam = Ops<FIXED>::div(dt, cell_m);
+          const float edge_volume = __fmul_rn(dt, cell_m);
+          const UpdateCtx uc{g, dry, lam, area, edge_volume, dt, scale, flags, nx, ny,
+                             apply, comp, manning, (flags & 15u) != 0u};
+          update_cell<FIXED>(uc, m.cell[warp + 1][lane + 1], hu, hv, apply ? src : 0.0f,
+                             comp ? resid : 0.0f, mn, m.fx[warp][lane], m.fx[warp][lane + 1],
+                             m.fy[warp][lane], m.fy[warp + 1][lane], X0 + lane, Y0 + warp, h2,
+                             mu, mv, residual, csrc, copn, crnd);
+          if (comp) out[3 * nn + gi] = residual;
+        } else {
+          out[3 * nn + gi] = comp ? resid : in[3 * nn + gi];
+        }
+        out[gi] = h2;
+        out[nn + gi] = mu;
+        out[2 * nn + gi] = mv;
+        // velocities() of the new state, and the records' speeds from the same quotients
+        // (cell_speeds: |u| + c and |v| + c).
+        const float4 c4 = velocities<FIXED>(h2, mu, mv, z, dry);
+        const float gh = __fmul_rn(g, h2);
+        const float cc = gh == 0.0f ? gh : Ops<FIXED>::sqrt(gh);
+        ga = __float_as_uint(__fadd_rn(fabsf(c4.z), cc));
+        gb = __float_as_uint(__fadd_rn(fabsf(c4.w), cc));
+        m.cell[warp + 1][lane + 1] = c4;
+        h = h2;
+        hu = mu;
+        hv = mv;
+        if (comp) resid = residual;
+      }
+      const int rslot = warp * kStrip + lane;
+      m.ring[rslot] = csrc;
+      m.ring[16 * kStrip + rslot] = copn;
+      m.ring[32 * kStrip + rslot] = crnd;
+      opn_seen = copn != 0.0f;
+      rnd_seen = crnd != 0.0f;
+      // 4. the block's two records (as block_item's)
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) {
+        ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
+        gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
+      }
+      const bool any_opn = __any_sync(0xffffffffu, opn_seen);
+      const bool any_rnd = __any_sync(0xffffffffu, rnd_seen);
+      if ((lane & 15) == 0) {
+        atomicMax(&m.ab[(lane >> 4) * 2], ga);
+        atomicMax(&m.ab[(lane >> 4) * 2 + 1], gb);
+      }
+      if (lane == 0 && (any_opn || any_rnd))
+        atomicOr(&m.need, (any_opn ? 1u : 0u) | (any_rnd ? 2u : 0u));
+      __syncthreads();
+      if (warp == 0) {
+        uint32_t ia = 0u, ib = 0u;
+        const uint32_t need = m.need;
+        group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16,
+                      m.ab[lane < 16 ? 0 : 2], m.ab[lane < 16 ? 1 : 3], m.ring,
+                      dt > 0.0f && apply, (need & 1u) != 0u, (need & 2u) != 0u, ia, ib);
+        if (lane == 0) {
+          atomicMax(&rc->slot[next].max_a, ia);
+          atomicMax(&rc->slot[next].max_b, ib);
+        }
+      }
+      __syncthreads();
+      resident_arrive(rc);
+      // The next tick's interior faces while the other CTAs finish this one.
+      if (k + 1u < ticks) interior_faces<FIXED, kBlkWideThreads>(m, rows, cols, g, hg);
     }
-    if (!resident_barrier(rc, n * (k + 1u))) return;
+    if (!resident_wait(rc, n * (k + 1u))) return;
     if (src_flag && every > 1u) phase = phase + 1u == every ? 0u : phase + 1u;
     cur ^= 1u;
     rec ^= 1u;
