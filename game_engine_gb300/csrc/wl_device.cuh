@@ -214,6 +214,24 @@ struct Ops {
   static __device__ __forceinline__ float cbrt(float h) { return cbrt_fixed(h); }
 };
 
+// The quotient and the root with zero taken apart (ZG): sqrt(+-0) is +-0 and 0 / b is 0 with a's
+// sign for b > 0, the same bits, without the intrinsics' slow path that a zero argument takes. A
+// tick where many arguments are zero (a still column, a wet/dry front) runs faster; elsewhere the
+// tests cost a little (the plain tick keeps the bare intrinsics).
+template <bool FIXED, bool ZG>
+__device__ __forceinline__ float zsqrt(float x) {
+  if (!ZG) return Ops<FIXED>::sqrt(x);
+  const float r = Ops<FIXED>::sqrt(x == 0.0f ? 1.0f : x);
+  return x == 0.0f ? x : r;
+}
+template <bool FIXED, bool ZG>
+__device__ __forceinline__ float zdiv(float a, float b) {
+  if (!ZG) return Ops<FIXED>::div(a, b);
+  const bool zero = a == 0.0f && b > 0.0f;
+  const float q = Ops<FIXED>::div(zero ? 1.0f : a, b);
+  return zero ? a : q;
+}
+
 // pressure (slang:186-191): (0.5 g) h h.
 __device__ __forceinline__ float pressure(float half_g, float h) {
   return __fmul_rn(__fmul_rn(half_g, h), h);
@@ -222,10 +240,9 @@ __device__ __forceinline__ float pressure(float half_g, float h) {
 // face (slang:274-292) over face_flux (slang:204-262): the face's bed the larger of the two, each
 // side reconstructed against it, the central-upwind flux between them, and the normal momentum's
 // flux less each side's pressure. Returns {h, nl, nr, t}.
-template <bool FIXED>
+template <bool FIXED, bool ZG = false>
 __device__ __forceinline__ float4 face(float g, float half_g, float hl0, float zl, float ul,
                                        float vl, float hr0, float zr, float ur, float vr) {
-  using O = Ops<FIXED>;
   const float zf = max2(zl, zr);
   const float el = __fsub_rn(__fadd_rn(hl0, zl), zf);
   const float er = __fsub_rn(__fadd_rn(hr0, zr), zf);
@@ -240,8 +257,8 @@ __device__ __forceinline__ float4 face(float g, float half_g, float hl0, float z
     fn = __fadd_rn(__fmul_rn(q, ul), pl);
     ft = __fmul_rn(q, vl);
   } else {
-    const float cl = O::sqrt(__fmul_rn(g, hl));
-    const float cr = O::sqrt(__fmul_rn(g, hr));
+    const float cl = zsqrt<FIXED, ZG>(__fmul_rn(g, hl));
+    const float cr = zsqrt<FIXED, ZG>(__fmul_rn(g, hr));
     const float ap = max2(max2(__fadd_rn(ur, cr), __fadd_rn(ul, cl)), 0.0f);
     const float am = min2(min2(__fsub_rn(ur, cr), __fsub_rn(ul, cl)), 0.0f);
     const float span = __fsub_rn(ap, am);
@@ -263,9 +280,9 @@ __device__ __forceinline__ float4 face(float g, float half_g, float hl0, float z
       const float t10 = __fadd_rn(__fsub_rn(__fmul_rn(ap, __fmul_rn(ql, vl)),
                                             __fmul_rn(am, __fmul_rn(qr, vr))),
                                   __fmul_rn(apam, t7));
-      fh = O::div(h6, span);
-      fn = O::div(n10, span);
-      ft = O::div(t10, span);
+      fh = zdiv<FIXED, ZG>(h6, span);
+      fn = zdiv<FIXED, ZG>(n10, span);
+      ft = zdiv<FIXED, ZG>(t10, span);
     }
   }
   return make_float4(fh, __fsub_rn(fn, pl), __fsub_rn(fn, pr), ft);

@@ -315,11 +315,11 @@ struct Item {
 };
 
 // {h, z, u, v} of a cell from its loaded h, hu, hv and bed (slang:303-314).
-template <bool FIXED>
+template <bool FIXED, bool ZG = false>
 __device__ __forceinline__ float4 velocities(float h, float hu, float hv, float z, float dry) {
   const bool wet = h >= dry;
-  const float u = wet ? Ops<FIXED>::div(hu, h) : 0.0f;
-  const float v = wet ? Ops<FIXED>::div(hv, h) : 0.0f;
+  const float u = wet ? zdiv<FIXED, ZG>(hu, h) : 0.0f;
+  const float v = wet ? zdiv<FIXED, ZG>(hv, h) : 0.0f;
   return make_float4(h, z, u, v);
 }
 
@@ -330,13 +330,13 @@ __device__ __forceinline__ float4 load_cell(const float* ph, const float* phu, c
 }
 
 // An x face between cells L and R; a y face between cells S and N (slang:274-292, 597-628).
-template <bool FIXED>
+template <bool FIXED, bool ZG = false>
 __device__ __forceinline__ float4 face_x(float g, float hg, const float4& L, const float4& R) {
-  return face<FIXED>(g, hg, L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w);
+  return face<FIXED, ZG>(g, hg, L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w);
 }
-template <bool FIXED>
+template <bool FIXED, bool ZG = false>
 __device__ __forceinline__ float4 face_y(float g, float hg, const float4& S, const float4& N) {
-  return face<FIXED>(g, hg, S.x, S.y, S.w, S.z, N.x, N.y, N.w, N.z);
+  return face<FIXED, ZG>(g, hg, S.x, S.y, S.w, S.z, N.x, N.y, N.w, N.z);
 }
 
 __device__ __forceinline__ float4 shfl_up4(const float4& v) {
@@ -1310,34 +1310,34 @@ __device__ __forceinline__ bool resident_barrier(ResidentCtl* rc, uint32_t targe
 // The faces of a 32 x 16 block whose cells are all the block's own (none on the halo): x faces
 // 1 .. cols - 1 of each row and y faces 1 .. rows - 1 of each column. A CTA computes the next
 // tick's while it waits at the barrier; the boundary faces need the halo, read after it.
-template <bool FIXED, int THREADS>
+template <bool FIXED, int THREADS, bool ZG>
 __device__ __forceinline__ void interior_faces(BlockSmem& m, int rows, int cols, float g,
                                                float hg) {
   const int nfx = rows * (cols - 1), nfy = (rows - 1) * cols;
   for (int q = threadIdx.x; q < nfx + nfy; q += THREADS) {
     if (q < nfx) {
       const int r = q / (cols - 1), f = q - r * (cols - 1) + 1;
-      m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
+      m.fx[r][f] = face_x<FIXED, ZG>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
     } else {
       const int q2 = q - nfx;
       const int f = q2 / cols + 1, c = q2 - (f - 1) * cols;
-      m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
+      m.fy[f][c] = face_y<FIXED, ZG>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
     }
   }
 }
 
 // The faces on the block's boundary (x faces 0 and cols, y faces 0 and rows), once the halo is in.
-template <bool FIXED>
+template <bool FIXED, bool ZG>
 __device__ __forceinline__ void boundary_faces(BlockSmem& m, int rows, int cols, float g,
                                                float hg) {
   const int q = threadIdx.x;
   if (q < 2 * rows) {
     const int r = q >> 1, f = (q & 1) ? cols : 0;
-    m.fx[r][f] = face_x<FIXED>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
+    m.fx[r][f] = face_x<FIXED, ZG>(g, hg, m.cell[r + 1][f], m.cell[r + 1][f + 1]);
   } else if (q < 2 * rows + 2 * cols) {
     const int q2 = q - 2 * rows;
     const int c = q2 >> 1, f = (q2 & 1) ? rows : 0;
-    m.fy[f][c] = face_y<FIXED>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
+    m.fy[f][c] = face_y<FIXED, ZG>(g, hg, m.cell[f][c + 1], m.cell[f + 1][c + 1]);
   }
 }
 
@@ -1385,10 +1385,10 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
     z = T.bed[gi];
     if (src_flag) src = T.source[gi];
     if (manning) mn = T.manning[gi];
-    m.cell[warp + 1][lane + 1] = velocities<FIXED>(h, hu, hv, z, dry);
+    m.cell[warp + 1][lane + 1] = velocities<FIXED, true>(h, hu, hv, z, dry);
   }
   __syncthreads();
-  if (!folder) interior_faces<FIXED, kBlkWideThreads>(m, rows, cols, g, hg);
+  if (!folder) interior_faces<FIXED, kBlkWideThreads, true>(m, rows, cols, g, hg);
   uint32_t slot = 0u;  // k % 3
   for (uint32_t k = 0; k < ticks; ++k) {
     // What the last tick left: the control block's at the first tick, the rotating slot after.
@@ -1430,7 +1430,8 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
       // 1. the halo (the neighbours' last tick, or a ghost of this block's own edge)
       const HaloCell hc = halo_cell(m, t, X0, Y0, rows, cols, nx, ny, flags);
       if (hc.slot != nullptr) {
-        float4 v = velocities<FIXED>(in[hc.i], in[nn + hc.i], in[2 * nn + hc.i], T.bed[hc.i], dry);
+        float4 v =
+            velocities<FIXED, true>(in[hc.i], in[nn + hc.i], in[2 * nn + hc.i], T.bed[hc.i], dry);
         if (hc.ghost) {
           if (hc.flip_v) v.w = __fmul_rn(hc.sign, v.w);
           else v.z = __fmul_rn(hc.sign, v.z);
@@ -1441,7 +1442,7 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
       const bool apply = src_flag && (every <= 1u || phase + 1u == every);
       __syncthreads();
       // 2. the boundary faces (the interior ones were taken while waiting at the last barrier)
-      if (dt > 0.0f) boundary_faces<FIXED>(m, rows, cols, g, hg);
+      if (dt > 0.0f) boundary_faces<FIXED, true>(m, rows, cols, g, hg);
       __syncthreads();
       // 3. the update, its speeds, and the next tick's velocities
       uint32_t ga = 0u, gb = 0u;
@@ -1470,7 +1471,7 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
         out[2 * nn + gi] = mv;
         // velocities() of the new state, and the records' speeds from the same quotients
         // (cell_speeds: |u| + c and |v| + c).
-        const float4 c4 = velocities<FIXED>(h2, mu, mv, z, dry);
+        const float4 c4 = velocities<FIXED, true>(h2, mu, mv, z, dry);
         const float gh = __fmul_rn(g, h2);
         const float cc = gh == 0.0f ? gh : Ops<FIXED>::sqrt(gh);
         ga = __float_as_uint(__fadd_rn(fabsf(c4.z), cc));
@@ -1516,7 +1517,7 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
       __syncthreads();
       resident_arrive(rc);
       // The next tick's interior faces while the other CTAs finish this one.
-      if (k + 1u < ticks) interior_faces<FIXED, kBlkWideThreads>(m, rows, cols, g, hg);
+      if (k + 1u < ticks) interior_faces<FIXED, kBlkWideThreads, true>(m, rows, cols, g, hg);
     }
     if (!resident_wait(rc, n * (k + 1u))) return;
     if (src_flag && every > 1u) phase = phase + 1u == every ? 0u : phase + 1u;
