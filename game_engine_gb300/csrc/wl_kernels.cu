@@ -1277,28 +1277,46 @@ __device__ __forceinline__ void resident_arrive(ResidentCtl* rc) {
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&rc->arrived) : "memory");
 }
 
-__device__ __forceinline__ bool resident_wait(ResidentCtl* rc, uint32_t target) {
-  __shared__ int s_ok;
+// Lane 0 of the CTA's first kPollers warps poll, staggered, so that the count's last step is seen
+// sooner than one poller's round trip; the first to see it tells the others through `s_seen`
+// (which holds the last count seen, so it needs no reset between ticks; zeroed at the launch's
+// start by resident_start).
+constexpr int kPollers = 4;
+__shared__ uint32_t s_seen;
+__shared__ int s_fail;
+
+__device__ __forceinline__ void resident_start() {
   if (threadIdx.x == 0) {
-    int ok = 1;
+    s_seen = 0u;
+    s_fail = 0;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool resident_wait(ResidentCtl* rc, uint32_t target) {
+  if ((threadIdx.x & 31) == 0 && threadIdx.x < 32 * kPollers) {
+    volatile uint32_t* seen = &s_seen;
     const uint64_t t0 = global_ns();
-    for (uint32_t polls = 1;; ++polls) {
+    for (uint32_t polls = 1; *seen < target; ++polls) {
       uint32_t c;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&rc->arrived) : "memory");
-      if (c >= target) break;
+      if (c >= target) {
+        *seen = target;
+        break;
+      }
       if ((polls & 63u) == 0u) {
         const uint32_t e = static_cast<const volatile ResidentCtl*>(rc)->error;
         if (e != 0u || global_ns() - t0 > kResidentWaitNs) {
           atomicOr(&rc->error, 1u);
-          ok = 0;
+          s_fail = 1;
+          *seen = target;  // the other pollers stop too
           break;
         }
       }
     }
-    s_ok = ok;
   }
   __syncthreads();
-  return s_ok != 0;
+  return s_fail == 0;
 }
 
 __device__ __forceinline__ bool resident_barrier(ResidentCtl* rc, uint32_t target) {
@@ -1341,12 +1359,16 @@ __device__ __forceinline__ void boundary_faces(BlockSmem& m, int rows, int cols,
   }
 }
 
+// The resident tick's CTA: a thread a cell. (A face a thread, at 1024 threads, was slower: 5.04
+// against 4.48 us a tick on the 256 x 256 tile.)
+constexpr int kResThreads = 512;
+
 template <bool FIXED, bool MANNING>
-__global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickArgs a,
-                                                                          uint32_t ticks,
-                                                                          ResidentCtl* rc) {
-  static_assert(kBlkWideThreads == kBlkW * kBlkH, "a thread a cell");
-  static_assert(kBlkWideThreads >= 2 * kBlkW + 2 * kBlkH, "a thread a boundary face");
+__global__ void __launch_bounds__(kResThreads, 1024 / kResThreads)
+    tick_resident_kernel(TickArgs a, uint32_t ticks, ResidentCtl* rc) {
+  static_assert(kResThreads >= kBlkW * kBlkH, "a thread a cell");
+  static_assert(kResThreads >= int(kGroupCells) && kResThreads >= 2 * kBlkW + 2 * kBlkH,
+                "a thread a virtual lane of the fold, and a boundary face");
   extern __shared__ float4 smem_raw[];
   BlockSmem& m = *reinterpret_cast<BlockSmem*>(smem_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -1387,8 +1409,8 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
     if (manning) mn = T.manning[gi];
     m.cell[warp + 1][lane + 1] = velocities<FIXED, true>(h, hu, hv, z, dry);
   }
-  __syncthreads();
-  if (!folder) interior_faces<FIXED, kBlkWideThreads, true>(m, rows, cols, g, hg);
+  resident_start();
+  if (!folder) interior_faces<FIXED, kResThreads, true>(m, rows, cols, g, hg);
   uint32_t slot = 0u;  // k % 3
   for (uint32_t k = 0; k < ticks; ++k) {
     // What the last tick left: the control block's at the first tick, the rotating slot after.
@@ -1482,10 +1504,12 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
         hv = mv;
         if (comp) resid = residual;
       }
-      const int rslot = warp * kStrip + lane;
-      m.ring[rslot] = csrc;
-      m.ring[16 * kStrip + rslot] = copn;
-      m.ring[32 * kStrip + rslot] = crnd;
+      if (warp < kBlkH) {
+        const int rslot = warp * kStrip + lane;
+        m.ring[rslot] = csrc;
+        m.ring[16 * kStrip + rslot] = copn;
+        m.ring[32 * kStrip + rslot] = crnd;
+      }
       opn_seen = copn != 0.0f;
       rnd_seen = crnd != 0.0f;
       // 4. the block's two records (as block_item's)
@@ -1517,7 +1541,7 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
       __syncthreads();
       resident_arrive(rc);
       // The next tick's interior faces while the other CTAs finish this one.
-      if (k + 1u < ticks) interior_faces<FIXED, kBlkWideThreads, true>(m, rows, cols, g, hg);
+      if (k + 1u < ticks) interior_faces<FIXED, kResThreads, true>(m, rows, cols, g, hg);
     }
     if (!resident_wait(rc, n * (k + 1u))) return;
     if (src_flag && every > 1u) phase = phase + 1u == every ? 0u : phase + 1u;
@@ -1544,6 +1568,7 @@ __global__ void __launch_bounds__(kBlkWideThreads, 2) tick_resident_kernel(TickA
 // others give up after the bound and mark the error word. The host zeroes `rc` and reads it.
 __global__ void resident_barrier_probe_kernel(ResidentCtl* rc, uint32_t n) {
   if (blockIdx.x + 1u == gridDim.x) return;  // the CTA that does not arrive
+  resident_start();
   resident_barrier(rc, n);
 }
 
@@ -1972,7 +1997,7 @@ int resident_capacity(bool fixed, bool manning) {
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return 0;
   int blocks = 0, device = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kBlkWideThreads, smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kResThreads, smem) !=
           cudaSuccess ||
       cudaGetDevice(&device) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
@@ -1991,7 +2016,7 @@ cudaError_t launch_tick_resident(bool fixed, bool manning, const TickArgs& args,
             : (manning ? tick_resident_kernel<false, true> : tick_resident_kernel<false, false>);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(a.n_items + 1u);
-  cfg.blockDim = dim3(kBlkWideThreads);
+  cfg.blockDim = dim3(kResThreads);
   cfg.dynamicSmemBytes = sizeof(BlockSmem);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
