@@ -63,7 +63,8 @@ class Tile(C.Structure):
 
 class Tuning(C.Structure):
     """wl_tuning: the batched launch's shape."""
-    _fields_ = [("block_rows", C.c_uint32), ("order", C.c_uint32), ("us_per_tick", C.c_float)]
+    _fields_ = [("block_rows", C.c_uint32), ("order", C.c_uint32), ("us_per_tick", C.c_float),
+                ("zero_apart", C.c_uint32)]
 
 
 class Event(C.Structure):

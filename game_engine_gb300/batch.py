@@ -180,16 +180,18 @@ class Batch:
         t = _abi.Tuning()
         self._check(lib().wl_batch_autotune(self._h, float(max_dt), int(trial_ticks), C.byref(t),
                                             self._buf, len(self._buf)))
-        return dict(block_rows=t.block_rows, order=t.order, us_per_tick=t.us_per_tick)
+        return dict(block_rows=t.block_rows, order=t.order, us_per_tick=t.us_per_tick,
+                    zero_apart=t.zero_apart)
 
-    def set_tuning(self, block_rows, order):
-        t = _abi.Tuning(int(block_rows), int(order), 0.0)
+    def set_tuning(self, block_rows, order, zero_apart=0):
+        t = _abi.Tuning(int(block_rows), int(order), 0.0, int(zero_apart))
         self._check(lib().wl_batch_set_tuning(self._h, C.byref(t), self._buf, len(self._buf)))
 
     def tuning(self):
         t = _abi.Tuning()
         self._check(lib().wl_batch_get_tuning(self._h, C.byref(t)))
-        return dict(block_rows=t.block_rows, order=t.order, us_per_tick=t.us_per_tick)
+        return dict(block_rows=t.block_rows, order=t.order, us_per_tick=t.us_per_tick,
+                    zero_apart=t.zero_apart)
 
     def stream(self):
         return lib().wl_batch_stream(self._h)

@@ -95,7 +95,7 @@ std::vector<uint32_t> item_order(const std::vector<wlc::TileSpec>& specs, uint32
 uint64_t launch_key(const wl_batch* b) {
   return (uint64_t(b->set.shape()) << 48) ^ (uint64_t(b->tuning.order) << 40) ^
          (uint64_t(b->set.grid()) << 8) ^ (b->set.any_manning() ? 1u : 0u) ^
-         (b->set.plain() ? 2u : 0u);
+         (b->set.plain() ? 2u : 0u) ^ (b->set.zero_apart() ? 4u : 0u);
 }
 
 void drop_graphs(wl_batch* b) {
@@ -132,7 +132,10 @@ bool cache_lookup(const std::string& key, wl_tuning* out) {
       std::istringstream in(line);
       std::string k;
       wl_tuning t{};
-      if (in >> k >> t.block_rows >> t.order >> t.us_per_tick) g_cache[k] = t;
+      if (in >> k >> t.block_rows >> t.order >> t.us_per_tick) {
+        if (!(in >> t.zero_apart)) t.zero_apart = 0;
+        g_cache[k] = t;
+      }
     }
     it = g_cache.find(key);
     if (it == g_cache.end()) return false;
@@ -146,7 +149,8 @@ void cache_store(const std::string& key, const wl_tuning& t) {
   g_cache[key] = t;
   if (const char* path = std::getenv("WLCUDA_TUNING_CACHE")) {
     std::ofstream f(path, std::ios::app);
-    f << key << " " << t.block_rows << " " << t.order << " " << t.us_per_tick << "\n";
+    f << key << " " << t.block_rows << " " << t.order << " " << t.us_per_tick << " "
+      << t.zero_apart << "\n";
   }
 }
 
@@ -204,6 +208,7 @@ int wl_batch_create(const wl_config* common, const wl_options* options, const wl
   b->tuning.block_rows = 16;
   b->tuning.order = 1;
   b->tuning.us_per_tick = 0.0f;
+  b->tuning.zero_apart = 0;
   std::string msg;
   if (!b->set.create(common->device, b->specs, b->options.ops == WL_OPS_FIXED,
                      shape_of_rows(b->tuning.block_rows), item_order(b->specs, b->tuning.order),
@@ -549,11 +554,12 @@ int wl_batch_set_tuning(wl_batch* b, const wl_tuning* t, char* err, size_t err_l
   if (t == nullptr ||
       (t->block_rows != 1 && t->block_rows != 4 && t->block_rows != 16 && t->block_rows != 32 &&
        t->block_rows != 64) ||
-      t->order > 1)
+      t->order > 1 || t->zero_apart > 1)
     return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: a tuning out of range");
   std::string msg;
   if (!b->set.reshape(shape_of_rows(t->block_rows), item_order(b->specs, t->order), &msg))
     return cuda_fail(err, err_len, msg);
+  b->set.set_zero_apart(t->zero_apart != 0);
   b->tuning = *t;
   drop_graphs(b);
   return WL_OK;
@@ -582,19 +588,26 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
     // writes is taken first and put back after.
     if (!b->set.snapshot(&msg)) return cuda_fail(err, err_len, msg);
     best.us_per_tick = std::numeric_limits<float>::infinity();
+    // The zero-apart variant exists for the march's native plain form (16, 32, 64 rows).
+    const bool zg_trial = b->options.ops != WL_OPS_FIXED && b->set.plain();
     for (uint32_t rows : {1u, 4u, 16u, 32u, 64u}) {
       for (uint32_t order : {0u, 1u}) {
-        if (!b->set.reshape(shape_of_rows(rows), item_order(b->specs, order), &msg) ||
-            !b->set.restore(&msg))
-          return cuda_fail(err, err_len, msg);
-        float warm = 0.0f, us = 0.0f;
-        if (!time_ticks(b, 1, max_dt, &warm, &msg) || !b->set.restore(&msg) ||
-            !time_ticks(b, trial_ticks, max_dt, &us, &msg))
-          return cuda_fail(err, err_len, msg);
-        if (us < best.us_per_tick) {
-          best.block_rows = rows;
-          best.order = order;
-          best.us_per_tick = us;
+        for (uint32_t zg : {0u, 1u}) {
+          if (zg == 1u && !(zg_trial && rows >= 16u)) continue;
+          if (!b->set.reshape(shape_of_rows(rows), item_order(b->specs, order), &msg) ||
+              !b->set.restore(&msg))
+            return cuda_fail(err, err_len, msg);
+          b->set.set_zero_apart(zg != 0u);
+          float warm = 0.0f, us = 0.0f;
+          if (!time_ticks(b, 1, max_dt, &warm, &msg) || !b->set.restore(&msg) ||
+              !time_ticks(b, trial_ticks, max_dt, &us, &msg))
+            return cuda_fail(err, err_len, msg);
+          if (us < best.us_per_tick) {
+            best.block_rows = rows;
+            best.order = order;
+            best.us_per_tick = us;
+            best.zero_apart = zg;
+          }
         }
       }
     }
@@ -604,6 +617,7 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
   }
   if (!b->set.reshape(shape_of_rows(best.block_rows), item_order(b->specs, best.order), &msg))
     return cuda_fail(err, err_len, msg);
+  b->set.set_zero_apart(best.zero_apart != 0u);
   b->tuning = best;
   drop_graphs(b);
   if (chosen != nullptr) *chosen = best;

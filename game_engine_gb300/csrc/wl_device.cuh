@@ -289,13 +289,13 @@ __device__ __forceinline__ float4 face(float g, float half_g, float hl0, float z
 }
 
 // |u| + c and |v| + c (slang:317-326).
-template <bool FIXED>
+template <bool FIXED, bool ZG = false>
 __device__ __forceinline__ void cell_speeds(float g, float dry, float h, float hu, float hv,
                                             float& ax, float& ay) {
   using O = Ops<FIXED>;
   const bool wet = h >= dry;
-  const float u = wet ? O::div(hu, h) : 0.0f;
-  const float v = wet ? O::div(hv, h) : 0.0f;
+  const float u = wet ? zdiv<FIXED, ZG>(hu, h) : 0.0f;
+  const float v = wet ? zdiv<FIXED, ZG>(hv, h) : 0.0f;
   // sqrt(+-0) is +-0: a dry cell's zero takes no square root (the intrinsic's special-case path
   // is its slow one, and most cells of a dry landscape are exactly zero).
   const float gh = __fmul_rn(g, h);

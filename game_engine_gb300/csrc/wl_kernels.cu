@@ -323,10 +323,10 @@ __device__ __forceinline__ float4 velocities(float h, float hu, float hv, float 
   return make_float4(h, z, u, v);
 }
 
-template <bool FIXED>
+template <bool FIXED, bool ZG = false>
 __device__ __forceinline__ float4 load_cell(const float* ph, const float* phu, const float* phv,
                                             const float* bed, int i, float dry) {
-  return velocities<FIXED>(ph[i], phu[i], phv[i], bed[i], dry);
+  return velocities<FIXED, ZG>(ph[i], phu[i], phv[i], bed[i], dry);
 }
 
 // An x face between cells L and R; a y face between cells S and N (slang:274-292, 597-628).
@@ -467,7 +467,7 @@ __device__ __forceinline__ void split_partials(float* ring, int ring_row0, int r
 // are rows ring_row0 .. ring_row0 + H - 1 of a 16-row item that the CTA's warps share; their
 // volumes go to the CTA's ring and the records are the CTA's (split_partials, then group_records
 // after the CTA's barrier).
-template <bool FIXED, bool MANNING, int H, bool SPLIT, bool PLAIN = false>
+template <bool FIXED, bool MANNING, int H, bool SPLIT, bool PLAIN = false, bool ZG = false>
 __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, float* ring,
                       int ring_row0, uint32_t* s_ab, uint32_t* s_need, uint32_t& ia,
                       uint32_t& ib) {
@@ -517,7 +517,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
         qhv[i] = hv0;
         out[3 * n + i] = in[3 * n + i];
         float ax, ay;
-        cell_speeds<FIXED>(g, dry, h0, hu0, hv0, ax, ay);
+        cell_speeds<FIXED, ZG>(g, dry, h0, hu0, hv0, ax, ay);
         ga = max(ga, __float_as_uint(ax));
         gb = max(gb, __float_as_uint(ay));
       }
@@ -546,21 +546,21 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
       const int row = (Y0 + j) * nx;
       float4 w;
       if (X0 > 0) {
-        w = load_cell<FIXED>(ph, phu, phv, bed, row + X0 - 1, dry);
+        w = load_cell<FIXED, ZG>(ph, phu, phv, bed, row + X0 - 1, dry);
       } else {
-        w = load_cell<FIXED>(ph, phu, phv, bed, row, dry);
+        w = load_cell<FIXED, ZG>(ph, phu, phv, bed, row, dry);
         w.z = __fmul_rn(sw, w.z);
       }
-      const float4 cl = load_cell<FIXED>(ph, phu, phv, bed, row + X0 + last, dry);
+      const float4 cl = load_cell<FIXED, ZG>(ph, phu, phv, bed, row + X0 + last, dry);
       float4 e;
       if (X0 + last + 1 < nx) {
-        e = load_cell<FIXED>(ph, phu, phv, bed, row + X0 + last + 1, dry);
+        e = load_cell<FIXED, ZG>(ph, phu, phv, bed, row + X0 + last + 1, dry);
       } else {
         e = cl;
         e.z = __fmul_rn(se, cl.z);
       }
       wm.west[j] = w;
-      wm.east[j] = face_x<FIXED>(g, hg, cl, e);
+      wm.east[j] = face_x<FIXED, ZG>(g, hg, cl, e);
     }
   }
   __syncwarp();
@@ -570,17 +570,17 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
   int i = Y0 * nx + gxc;
   float hu = phu[i], hv = phv[i];
   float src = it.apply_source ? source[i] : 0.0f;
-  float4 c = velocities<FIXED>(ph[i], hu, hv, bed[i], dry);
+  float4 c = velocities<FIXED, ZG>(ph[i], hu, hv, bed[i], dry);
   float4 fs;
   {
     float4 s;
     if (Y0 > 0) {
-      s = load_cell<FIXED>(ph, phu, phv, bed, i - nx, dry);
+      s = load_cell<FIXED, ZG>(ph, phu, phv, bed, i - nx, dry);
     } else {
       s = c;
       s.w = __fmul_rn(ss, c.w);
     }
-    fs = face_y<FIXED>(g, hg, s, c);
+    fs = face_y<FIXED, ZG>(g, hg, s, c);
   }
   float nh = 0.0f, nhu = 0.0f, nhv = 0.0f, nz = 0.0f, nsrc = 0.0f;
   if (Y0 + 1 < ny) {
@@ -611,7 +611,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
     float4 nc;
     const float hu_n = nhu, hv_n = nhv, src_n = nsrc;
     if (gy + 1 < ny) {
-      nc = velocities<FIXED>(nh, nhu, nhv, nz, dry);
+      nc = velocities<FIXED, ZG>(nh, nhu, nhv, nz, dry);
     } else {
       nc = c;
       nc.w = __fmul_rn(sn, c.w);
@@ -625,10 +625,10 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
       nz = bed[k];
       if (src_on) nsrc = source[k];
     }
-    const float4 fn = face_y<FIXED>(g, hg, c, nc);
+    const float4 fn = face_y<FIXED, ZG>(g, hg, c, nc);
     float4 w = shfl_up4(c);
     if (lane == 0) w = wm.west[j];
-    const float4 fw = face_x<FIXED>(g, hg, w, c);
+    const float4 fw = face_x<FIXED, ZG>(g, hg, w, c);
     float4 fe = shfl_down4(fw);
     if (lane == last) fe = wm.east[j];
 
@@ -643,7 +643,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
       out[n32 + uint32_t(i)] = mu;
       out[2u * n32 + uint32_t(i)] = mv;
       if (comp) out[3 * n + i] = residual;
-      cell_speeds<FIXED>(g, dry, h, mu, mv, ax, ay);
+      cell_speeds<FIXED, ZG>(g, dry, h, mu, mv, ax, ay);
     }
     ga = max(ga, __float_as_uint(ax));
     gb = max(gb, __float_as_uint(ay));
@@ -684,7 +684,7 @@ __device__ void march(const TileDesc& T, const Item& it, const WarpMem<H>& wm, f
 // shared ring, the records by warp 0 after a barrier), so that the launch's last round is a
 // quarter of an item long instead of a whole one. The CTA's warps meet here when the whole items
 // run out. Out of line: the whole-item march keeps its registers.
-template <bool FIXED, bool MANNING, bool PLAIN>
+template <bool FIXED, bool MANNING, bool PLAIN, bool ZG>
 __device__ __noinline__ void tail_items(TickArgs a, const WarpMem<16> wm) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ uint32_t s_item, s_need;
@@ -738,7 +738,7 @@ __device__ __noinline__ void tail_items(TickArgs a, const WarpMem<16> wm) {
       __syncwarp();
     }
     uint32_t ia = 0u, ib = 0u;
-    march<FIXED, MANNING, 4, true, PLAIN>(T, it, w4, ring, 4 * warp, s_ab, &s_need, ia, ib);
+    march<FIXED, MANNING, 4, true, PLAIN, ZG>(T, it, w4, ring, 4 * warp, s_ab, &s_need, ia, ib);
     __syncthreads();
     if (warp == 0) {
       const uint32_t ga = s_ab[lane < 16 ? 0 : 2], gb = s_ab[lane < 16 ? 1 : 3];
@@ -754,8 +754,9 @@ __device__ __noinline__ void tail_items(TickArgs a, const WarpMem<16> wm) {
 
 // The persistent tick: every work item of every tile, one tick. PLAIN (no tile holds a flag of
 // kFlagsNotPlain) compiles the open edges, the compensated source and Manning out of the march,
-// which then fits 80 registers: six CTAs an SM instead of five.
-template <bool FIXED, bool MANNING, int H, bool PLAIN>
+// which then fits 80 registers: six CTAs an SM instead of five. ZG takes zero arguments apart
+// from the divisions and square roots (zsqrt, zdiv), a choice of the batches' autotuner.
+template <bool FIXED, bool MANNING, int H, bool PLAIN, bool ZG = false>
 __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickArgs a) {
   dependent_grid_start();
   if (a.go != nullptr && *a.go == 0u) return;
@@ -799,7 +800,7 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
       __syncwarp();
     }
     uint32_t ia = 0u, ib = 0u;
-    march<FIXED, MANNING, H, false, PLAIN>(T, it, wm, wm.ring, 0, nullptr, nullptr, ia, ib);
+    march<FIXED, MANNING, H, false, PLAIN, ZG>(T, it, wm, wm.ring, 0, nullptr, nullptr, ia, ib);
     __syncwarp();
     // `rec` read again rather than held through the march (a register fewer): only the tile's
     // last item flips it, after this item's count.
@@ -807,7 +808,7 @@ __global__ void __launch_bounds__(kCtaThreads, PLAIN ? 6 : 5) tick_kernel(TickAr
     __syncwarp();
   }
   if constexpr (H == 16) {
-    if (a.n_whole < a.n_items) tail_items<FIXED, MANNING, PLAIN>(a, wm);  // the same in every CTA
+    if (a.n_whole < a.n_items) tail_items<FIXED, MANNING, PLAIN, ZG>(a, wm);  // the same in every CTA
   }
   if (lane == 0 && slots < a.n_items) {  // the counters were read: the last warp out resets them
     __threadfence();
@@ -1867,11 +1868,15 @@ const void* tick_fn(bool fixed, bool manning, bool plain) {
 template <int H>
 cudaError_t tick_launch(bool fixed, bool manning, bool plain, const TickArgs& a, int grid,
                         cudaStream_t s) {
+  // The zero-apart variant: the native arithmetic's plain march only (the fixed form's quotient
+  // and root have no slow path to skip).
+  const bool zg = a.zero_apart != 0u && !fixed && !manning && plain;
   void (*k)(TickArgs) =
       fixed ? (manning ? tick_kernel<true, true, H, false>
                        : plain ? tick_kernel<true, false, H, true> : tick_kernel<true, false, H, false>)
             : (manning ? tick_kernel<false, true, H, false>
-                       : plain ? tick_kernel<false, false, H, true>
+                       : plain ? (zg ? tick_kernel<false, false, H, true, true>
+                                     : tick_kernel<false, false, H, true>)
                                : tick_kernel<false, false, H, false>);
   return launch_dependent(k, dim3(grid), dim3(kCtaThreads), kWarpsPerCta * WarpMem<H>::kBytes, s,
                           a);

@@ -27,6 +27,9 @@ struct TickArgs {
   // The block shape, one tile: the grid's last CTA folds the tile's ledger instead of item 0
   // (the launch holds one CTA more than items).
   uint32_t fold_apart = 0;
+  // The march's native plain variant with zero arguments taken apart from its divisions and
+  // square roots (the same bits; faster where many arguments are zero, slower where few are).
+  uint32_t zero_apart = 0;
 };
 
 // The block of cells one work item steps: 32 columns by 16, 32 or 64 rows, one warp marching

@@ -338,6 +338,7 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   a.n_items = n_items_;
   a.max_dt = max_dt;
   a.go = go;
+  a.zero_apart = zero_apart_ ? 1u : 0u;
   const bool manning = any_manning(), plain_set = plain();
   // The block shape's wide CTA where the launch holds no more blocks than the device has SMs; for
   // one tile, one CTA more folds its ledger beside the items.
@@ -370,6 +371,7 @@ cudaError_t TileSet::enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_
   a.work = d_work_ + 1 + tile;
   a.n_items = host_[tile].items;
   a.max_dt = max_dt;
+  a.zero_apart = zero_apart_ ? 1u : 0u;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
   const bool manning = (host_[tile].flags & kFlagManning) != 0u;

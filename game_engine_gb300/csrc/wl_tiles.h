@@ -46,6 +46,10 @@ class TileSet {
                             const uint32_t* go = nullptr);
   // Tick kernel launches enqueued since create (a diagnosis counter).
   uint64_t tick_launches() const { return tick_launches_; }
+  // The march's zero-apart variant for the set's launches (TickArgs::zero_apart; the autotuner's
+  // knob). The same bits either way.
+  void set_zero_apart(bool on) { zero_apart_ = on; }
+  bool zero_apart() const { return zero_apart_; }
   // One tile's own tick (the per-tile-launch form): only that tile's work items.
   cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);
   cudaError_t enqueue_prime(cudaStream_t s);
@@ -130,6 +134,7 @@ class TileSet {
   int resident_cap_[2] = {0, 0};  // resident CTAs the device holds (without, with Manning's)
   bool resident_used_ = false;      // a resident launch since the last wait()
   uint64_t tick_launches_ = 0;
+  bool zero_apart_ = false;
   uint32_t* d_item_tile_ = nullptr;  // the tile of each work item (null for one tile)
   uint32_t n_items_ = 0;
   int grid_ = 0;

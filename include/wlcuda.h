@@ -221,11 +221,16 @@ typedef struct wl_tile {
 /* The launch's shape: the rows one warp marches down a 32-column work item (16, 32 or 64; 4, 32 x
  * 16 items split over four warps of a CTA; 1, 32 x 16 items stepped by a CTA in three phases
  * through shared memory), the order items are dealt (0 tiles by index, 1 the largest tiles
- * first), and the trial's time a tick. */
+ * first), and the trial's time a tick. zero_apart (16, 32 and 64 rows, native ops, no Manning, no
+ * open edge, no compensated source): 1 takes a zero argument of the march's divisions and square
+ * roots apart from the IEEE intrinsic (sqrt(+-0) = +-0, 0 / b = +-0 for b > 0), the same bits
+ * without the intrinsic's slow path: faster where many arguments are zero (dry land, wet/dry
+ * fronts, still columns), slower where few are; the autotuner tries both. */
 typedef struct wl_tuning {
   uint32_t block_rows;
   uint32_t order;
   float us_per_tick;
+  uint32_t zero_apart;
 } wl_tuning;
 
 /* `common` gives cell_m, gravity, cfl, dry_depth_m and device (its nx, ny and edges are unused). */

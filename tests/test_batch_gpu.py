@@ -108,6 +108,28 @@ def test_autotune_leaves_the_state_as_it_was(gpu):
     assert c.autotune(0.02, trial_ticks=3) == chosen
 
 
+@pytest.mark.parametrize("rows", [16, 32, 64])
+def test_zero_apart_gives_the_same_bytes(gpu, rows):
+    """The march's zero-apart variant (the autotuner's knob) on a plain batch of the batched
+    configuration's tiles (dry land, a column each: zero depths and momenta everywhere): every
+    tile's bytes equal the bare intrinsics' after 120 ticks, and sampled tiles the oracle's."""
+    tiles = workloads.tiles_4096(24)
+    sides = [(t.nx, t.ny) for t in tiles]
+    out = []
+    for zg in (0, 1):
+        b = Batch(sides)
+        b.set_tuning(rows, 1, zero_apart=zg)
+        assert b.tuning()["zero_apart"] == zg
+        load(b, tiles, source=False)
+        b.run_ticks(120, 0.01)
+        out.append(b.tile_hashes())
+        b.close()
+    assert np.array_equal(out[0], out[1])
+    for k in (0, 11, 23):
+        r = oracle_tile(tiles[k], 0, 120, 0.01, source=False)
+        assert int(out[1][k]) == r.state_hash(), f"tile {k} {sides[k]}"
+
+
 def test_tiles_configuration_sample(gpu):
     # The batched configuration's tile-size distribution, 48 tiles, 200 ticks: every tile's
     # hash against the oracle.
