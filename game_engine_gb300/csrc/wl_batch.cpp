@@ -154,6 +154,9 @@ void cache_store(const std::string& key, const wl_tuning& t) {
   }
 }
 
+// The untimed ticks an autotuner trial steps before it times.
+constexpr uint32_t kTrialWarmTicks = 8;
+
 bool time_ticks(wl_batch* b, uint32_t ticks, float max_dt, float* us, std::string* msg) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -598,8 +601,11 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
               !b->set.restore(&msg))
             return cuda_fail(err, err_len, msg);
           b->set.set_zero_apart(zg != 0u);
+          // Each trial steps the same state past its first ticks untimed (a state as written is
+          // often still: zero momenta, which flatter the zero-apart variant) and times the next
+          // ones; every tuning steps to the same bytes, so each times the same ticks.
           float warm = 0.0f, us = 0.0f;
-          if (!time_ticks(b, 1, max_dt, &warm, &msg) || !b->set.restore(&msg) ||
+          if (!time_ticks(b, kTrialWarmTicks, max_dt, &warm, &msg) ||
               !time_ticks(b, trial_ticks, max_dt, &us, &msg))
             return cuda_fail(err, err_len, msg);
           if (us < best.us_per_tick) {

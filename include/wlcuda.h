@@ -293,9 +293,10 @@ int wl_batch_tile_hashes(wl_batch* batch, uint64_t* out, uint32_t count, char* e
 int wl_batch_read_ledgers(wl_batch* batch, wl_ledger* out, uint32_t count, char* err,
                           size_t err_len);
 
-/* The autotuner: times every block shape and item order on the batch itself for `trial_ticks`
- * ticks (the trials are undone), keeps the fastest, and caches it per (SM count, tile-size
- * histogram) for the process (and across processes in the file WLCUDA_TUNING_CACHE names). */
+/* The autotuner: times every block shape, item order and (on a plain native batch) zero_apart on
+ * the batch itself, each trial stepping 8 ticks untimed and then timing `trial_ticks` (the trials
+ * are undone), keeps the fastest, and caches it per (SM count, tile-size histogram) for the
+ * process (and across processes in the file WLCUDA_TUNING_CACHE names). */
 int wl_batch_autotune(wl_batch* batch, float max_dt, uint32_t trial_ticks, wl_tuning* chosen,
                       char* err, size_t err_len);
 int wl_batch_set_tuning(wl_batch* batch, const wl_tuning* tuning, char* err, size_t err_len);
