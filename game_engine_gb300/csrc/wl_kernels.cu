@@ -256,22 +256,17 @@ __device__ __forceinline__ float group_tree(const float* ring, int gc) {
   return c;
 }
 
-// The records of the two groups a warp covers in one group row (slang:338-371). `ga`/`gb` are
-// each lane's largest speeds over the group row; the ring holds the volumes of its 16 rows (rows
-// past the grid's edge zero). need_* names the quantities some cell holds. Returns the two groups'
-// largest speeds (lane 0 holds them).
-__device__ __forceinline__ void group_records(uint32_t groups_x, uint32_t groups_y,
-                                              Partial* rec_out, int X0, int group_row,
-                                              uint32_t ga, uint32_t gb, const float* ring,
-                                              bool need_src, bool need_opn, bool need_rnd,
-                                              uint32_t& ia, uint32_t& ib) {
+// The records of the two groups a warp covers in one group row (slang:338-371), the groups'
+// largest speeds given: (ga, gb) the west group's, (a1, b1) the east group's. The ring holds the
+// volumes of the group row's 16 rows (rows past the grid's edge zero); need_* names the quantities
+// some cell holds. Lane 0 writes the records and adds the two groups' speeds to ia, ib.
+__device__ __forceinline__ void write_group_records(uint32_t groups_x, uint32_t groups_y,
+                                                    Partial* rec_out, int X0, int group_row,
+                                                    uint32_t ga, uint32_t gb, uint32_t a1,
+                                                    uint32_t b1, const float* ring,
+                                                    bool need_src, bool need_opn, bool need_rnd,
+                                                    uint32_t& ia, uint32_t& ib) {
   const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int o = 8; o > 0; o >>= 1) {
-    ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
-    gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
-  }
-  const uint32_t a1 = __shfl_sync(0xffffffffu, ga, 16), b1 = __shfl_sync(0xffffffffu, gb, 16);
   float s0 = 0.0f, s1 = 0.0f, o0 = 0.0f, o1 = 0.0f, r0 = 0.0f, r1 = 0.0f;
   if (need_src) {
     s0 = group_tree(ring, 0);
@@ -304,6 +299,22 @@ __device__ __forceinline__ void group_records(uint32_t groups_x, uint32_t groups
     ib = max(ib, max(gb, b1));
   }
   __syncwarp();
+}
+// The same from each lane's largest speeds over the group row (lanes 0-15 the west group's,
+// 16-31 the east group's).
+__device__ __forceinline__ void group_records(uint32_t groups_x, uint32_t groups_y,
+                                              Partial* rec_out, int X0, int group_row,
+                                              uint32_t ga, uint32_t gb, const float* ring,
+                                              bool need_src, bool need_opn, bool need_rnd,
+                                              uint32_t& ia, uint32_t& ib) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) {
+    ga = max(ga, __shfl_xor_sync(0xffffffffu, ga, o));
+    gb = max(gb, __shfl_xor_sync(0xffffffffu, gb, o));
+  }
+  const uint32_t a1 = __shfl_sync(0xffffffffu, ga, 16), b1 = __shfl_sync(0xffffffffu, gb, 16);
+  write_group_records(groups_x, groups_y, rec_out, X0, group_row, ga, gb, a1, b1, ring, need_src,
+                      need_opn, need_rnd, ia, ib);
 }
 
 // ---- the march ------------------------------------------------------------------------------
@@ -1535,15 +1546,16 @@ __global__ void __launch_bounds__(kResThreads, 1024 / kResThreads)
       if (warp == 0) {
         uint32_t ia = 0u, ib = 0u;
         const uint32_t need = m.need;
-        group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16,
-                      m.ab[lane < 16 ? 0 : 2], m.ab[lane < 16 ? 1 : 3], m.ring,
-                      dt > 0.0f && apply, (need & 1u) != 0u, (need & 2u) != 0u, ia, ib);
+        write_group_records(T.groups_x, T.groups_y, T.rec[rec ^ 1u], X0, Y0 / 16, m.ab[0],
+                            m.ab[1], m.ab[2], m.ab[3], m.ring, dt > 0.0f && apply,
+                            (need & 1u) != 0u, (need & 2u) != 0u, ia, ib);
         if (lane == 0) {
           atomicMax(&rc->slot[next].max_a, ia);
           atomicMax(&rc->slot[next].max_b, ib);
         }
       }
-      __syncthreads();
+      // Thread 0 wrote the records and the speeds itself and saw every other thread's state
+      // through the barrier above: its release covers them, and the other warps go on.
       resident_arrive(rc);
       // The next tick's interior faces while the other CTAs finish this one.
       if (k + 1u < ticks) interior_faces<FIXED, kResThreads, true>(m, rows, cols, g, hg);
