@@ -1262,20 +1262,30 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
 
 // ---- the resident tick: many ticks of one small tile in one launch ----------------------------
 //
-// A tile of no more blocks than the device holds CTAs of the wide block tick (the 256 x 256 tile's
-// 128) steps `ticks` ticks in one cooperative launch: a CTA a block for the whole launch, one CTA
-// more for the ledger's fold, and a grid barrier between ticks in place of the launch boundary.
-// Each tick is the block tick's own (block_item, fold_ledger: the same arithmetic, records and
-// ledger). What the launches' flips would do tick by tick is kept in registers (the copy and the
-// record slot follow the ticks' parity, the source's clock its count) and the largest speeds in
-// three rotating slots of the ResidentCtl (tick k reads slot k % 3, adds to slot (k + 1) % 3, and
-// the fold's CTA clears slot (k + 2) % 3, read at tick k - 1); after the last tick CTA 0 writes the
-// control block as the last launch's flip would have left it.
+// A tile of no more blocks than the device has SMs (the 256 x 256 tile's 128) steps `ticks` ticks
+// in one cooperative launch: a 512-thread CTA a 32 x 16 block for the whole launch (a thread a
+// cell), one CTA more for the ledger's fold (fold_ledger), and a grid barrier between ticks in
+// place of the launch boundary. A tick is the block tick's three phases with the same per-cell
+// functions (velocities, face_x/face_y, update_cell, the records' trees), so the arithmetic,
+// records and ledger are the per-tick launch's. The block's own cells stay in registers (h, hu,
+// hv, the bed, the source, plane 3) and in the shared cell array ({h, z, u, v}) from tick to tick;
+// only the one-cell halo is read back, from the neighbours' output copy, after the barrier. The
+// interior faces (both cells the block's own, about 90 % of them) need nothing from the
+// neighbours, so a CTA computes the next tick's while it waits at the barrier.
 //
-// The barrier: each CTA's thread 0 adds one to `arrived` with release semantics and polls it
-// with acquire semantics until it reaches the tick's count (the host zeroes it before a launch).
-// A wait is bounded: past kResidentWaitNs it marks the error word and the CTA leaves, and so
-// does every CTA that then sees the mark, so the launch ends; the host reads the word.
+// What the launches' flips would do tick by tick is kept in registers (the copy and the record
+// slot follow the ticks' parity, the source's clock its count), and the tick's inputs in three
+// rotating slots of the ResidentCtl: tick k reads slot k % 3 (the largest speeds of the last
+// update, the ledger's time left), the blocks add their speeds to slot (k + 1) % 3 and the fold's
+// CTA writes its time left there, and the fold's CTA clears slot (k + 2) % 3, read at tick k - 1;
+// after the last tick CTA 0 writes the control block as the last launch's flip would have left it.
+//
+// The barrier: each CTA's thread 0 adds one to `arrived` with release semantics once its records
+// are written (the CTA barrier before them ordered every thread's state first), and lane 0 of the
+// first kPollers warps poll it with acquire semantics until it reaches the tick's count (the host
+// zeroes the words before a launch). A wait is bounded: past kResidentWaitNs it marks the error
+// word and the CTA leaves, and so does every CTA that then sees the mark, so the launch ends; the
+// host reads the word.
 constexpr uint64_t kResidentWaitNs = 1000000000ull;  // a second
 
 __device__ __forceinline__ uint64_t global_ns() {
