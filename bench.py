@@ -2,8 +2,8 @@
 """Benchmark of the live-water tick on a GB300 (one JSON line on stdout).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload plain_2048|plain_256|tiles_4096|adjoint_512|tiles_256_adjoint|
-                               tick_queue|full_step]
+                    [--workload plain_2048|plain_256|plain_1024|tiles_4096|adjoint_512|
+                               tiles_256_adjoint|tick_queue|full_step]
 
 The metric is water cell-updates per second. A bench step is one pass of the workload over its
 configuration: for the default (plain_2048, the throughput configuration) 500 ticks of one
@@ -753,6 +753,10 @@ def main():
         tile = workloads.plain_2048(terrain=terrain)
     elif args.workload == "plain_256":
         tile = workloads.plain_256(terrain=terrain)
+    elif args.workload == "plain_1024":
+        # The throughput tile's terrain, depth and rain at 1024 x 1024: a tile of the three-phase
+        # block shape in 256-thread CTAs (2048 blocks), the staged block tick's, for a profiler.
+        tile = workloads.plain_2048(1024, terrain=terrain)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     if args.ticks > 0:

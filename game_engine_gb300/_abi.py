@@ -64,7 +64,7 @@ class Tile(C.Structure):
 class Tuning(C.Structure):
     """wl_tuning: the batched launch's shape."""
     _fields_ = [("block_rows", C.c_uint32), ("order", C.c_uint32), ("us_per_tick", C.c_float),
-                ("zero_apart", C.c_uint32)]
+                ("zero_apart", C.c_uint32), ("stage", C.c_uint32)]
 
 
 class Event(C.Structure):
@@ -128,6 +128,7 @@ SIGNATURES = {
     "wl_cell_count": (C.c_uint32, [C.c_void_p]),
     "wl_group_count": (C.c_uint32, [C.c_void_p]),
     "wl_tick_launches": (C.c_uint64, [C.c_void_p]),
+    "wl_staged_tiles": (C.c_uint32, [C.c_void_p]),
     "wl_resident_barrier_check": (C.c_int, [C.c_int, C.c_uint32, C.c_char_p, C.c_size_t]),
     "wl_write_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
     "wl_read_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, *_err]),
@@ -155,6 +156,7 @@ SIGNATURES = {
     "wl_batch_destroy": (None, [C.c_void_p]),
     "wl_batch_tile_count": (C.c_uint32, [C.c_void_p]),
     "wl_batch_cell_count": (C.c_uint64, [C.c_void_p]),
+    "wl_batch_staged_tiles": (C.c_uint32, [C.c_void_p]),
     "wl_batch_tile_first": (C.c_uint64, [C.c_void_p, C.c_uint32]),
     "wl_batch_settled": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_size_t, C.c_float, C.c_float,
                                    C.POINTER(C.c_uint8), C.POINTER(C.c_float),

@@ -181,20 +181,24 @@ class Batch:
         self._check(lib().wl_batch_autotune(self._h, float(max_dt), int(trial_ticks), C.byref(t),
                                             self._buf, len(self._buf)))
         return dict(block_rows=t.block_rows, order=t.order, us_per_tick=t.us_per_tick,
-                    zero_apart=t.zero_apart)
+                    zero_apart=t.zero_apart, stage=t.stage)
 
-    def set_tuning(self, block_rows, order, zero_apart=0):
-        t = _abi.Tuning(int(block_rows), int(order), 0.0, int(zero_apart))
+    def set_tuning(self, block_rows, order, zero_apart=0, stage=0):
+        t = _abi.Tuning(int(block_rows), int(order), 0.0, int(zero_apart), int(stage))
         self._check(lib().wl_batch_set_tuning(self._h, C.byref(t), self._buf, len(self._buf)))
 
     def tuning(self):
         t = _abi.Tuning()
         self._check(lib().wl_batch_get_tuning(self._h, C.byref(t)))
         return dict(block_rows=t.block_rows, order=t.order, us_per_tick=t.us_per_tick,
-                    zero_apart=t.zero_apart)
+                    zero_apart=t.zero_apart, stage=t.stage)
 
     def stream(self):
         return lib().wl_batch_stream(self._h)
+
+    def staged_tiles(self):
+        """Tiles whose blocks the batch's launches take by tensor copies under its tuning."""
+        return int(lib().wl_batch_staged_tiles(self._h))
 
 
 def concat(tiles, field):

@@ -142,6 +142,14 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
     delete s;
     return cuda_fail(err, err_len, msg);
   }
+  // The block shape's staged variant (a block's cells and halo by tensor copies, where the tile's
+  // width is a multiple of 4): by default in the 256-thread block CTA only; WLCUDA_STAGE=1 in both
+  // block CTAs, 0 in neither. The same bytes either way.
+  s->set.set_stage(wlc::TileSet::kStageAuto);
+  if (const char* stage = std::getenv("WLCUDA_STAGE")) {
+    if (std::strcmp(stage, "0") == 0) s->set.set_stage(wlc::TileSet::kStageOff);
+    if (std::strcmp(stage, "1") == 0) s->set.set_stage(wlc::TileSet::kStageOn);
+  }
   s->cells = config->nx * config->ny;
   s->groups = ((config->nx + 15) / 16) * ((config->ny + 15) / 16);
   *out = s;
@@ -164,6 +172,10 @@ uint32_t wl_group_count(const wl_step* step) { return valid(step) ? step->groups
 
 uint64_t wl_tick_launches(const wl_step* step) {
   return valid(step) ? step->set.tick_launches() : 0u;
+}
+
+uint32_t wl_staged_tiles(const wl_step* step) {
+  return valid(step) ? step->set.staged_launch_tiles() : 0u;
 }
 
 int wl_write_state(wl_step* s, const double* h, const double* hu, const double* hv, size_t n,

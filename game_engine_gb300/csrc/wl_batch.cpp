@@ -95,7 +95,7 @@ std::vector<uint32_t> item_order(const std::vector<wlc::TileSpec>& specs, uint32
 uint64_t launch_key(const wl_batch* b) {
   return (uint64_t(b->set.shape()) << 48) ^ (uint64_t(b->tuning.order) << 40) ^
          (uint64_t(b->set.grid()) << 8) ^ (b->set.any_manning() ? 1u : 0u) ^
-         (b->set.plain() ? 2u : 0u) ^ (b->set.zero_apart() ? 4u : 0u);
+         (b->set.plain() ? 2u : 0u) ^ (b->set.zero_apart() ? 4u : 0u) ^ (b->set.stage() != 0u ? 8u : 0u);
 }
 
 void drop_graphs(wl_batch* b) {
@@ -134,6 +134,7 @@ bool cache_lookup(const std::string& key, wl_tuning* out) {
       wl_tuning t{};
       if (in >> k >> t.block_rows >> t.order >> t.us_per_tick) {
         if (!(in >> t.zero_apart)) t.zero_apart = 0;
+        if (!(in >> t.stage)) t.stage = 0;
         g_cache[k] = t;
       }
     }
@@ -150,7 +151,7 @@ void cache_store(const std::string& key, const wl_tuning& t) {
   if (const char* path = std::getenv("WLCUDA_TUNING_CACHE")) {
     std::ofstream f(path, std::ios::app);
     f << key << " " << t.block_rows << " " << t.order << " " << t.us_per_tick << " "
-      << t.zero_apart << "\n";
+      << t.zero_apart << " " << t.stage << "\n";
   }
 }
 
@@ -212,6 +213,7 @@ int wl_batch_create(const wl_config* common, const wl_options* options, const wl
   b->tuning.order = 1;
   b->tuning.us_per_tick = 0.0f;
   b->tuning.zero_apart = 0;
+  b->tuning.stage = 0;
   std::string msg;
   if (!b->set.create(common->device, b->specs, b->options.ops == WL_OPS_FIXED,
                      shape_of_rows(b->tuning.block_rows), item_order(b->specs, b->tuning.order),
@@ -234,6 +236,10 @@ void wl_batch_destroy(wl_batch* b) {
 uint32_t wl_batch_tile_count(const wl_batch* b) { return valid(b) ? b->set.tile_count() : 0u; }
 
 uint64_t wl_batch_cell_count(const wl_batch* b) { return valid(b) ? b->set.total_cells() : 0u; }
+
+uint32_t wl_batch_staged_tiles(const wl_batch* b) {
+  return valid(b) ? b->set.staged_launch_tiles() : 0u;
+}
 
 uint64_t wl_batch_tile_first(const wl_batch* b, uint32_t tile) {
   return valid(b) && tile < b->set.tile_count() ? b->set.first_cell(tile) : 0u;
@@ -557,12 +563,13 @@ int wl_batch_set_tuning(wl_batch* b, const wl_tuning* t, char* err, size_t err_l
   if (t == nullptr ||
       (t->block_rows != 1 && t->block_rows != 4 && t->block_rows != 16 && t->block_rows != 32 &&
        t->block_rows != 64) ||
-      t->order > 1 || t->zero_apart > 1)
+      t->order > 1 || t->zero_apart > 1 || t->stage > 1)
     return fail(err, err_len, WL_ERR_ARGUMENT, "water_live: a tuning out of range");
   std::string msg;
   if (!b->set.reshape(shape_of_rows(t->block_rows), item_order(b->specs, t->order), &msg))
     return cuda_fail(err, err_len, msg);
   b->set.set_zero_apart(t->zero_apart != 0);
+  b->set.set_stage(t->stage != 0u ? wlc::TileSet::kStageOn : wlc::TileSet::kStageOff);
   b->tuning = *t;
   drop_graphs(b);
   return WL_OK;
@@ -593,14 +600,18 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
     best.us_per_tick = std::numeric_limits<float>::infinity();
     // The zero-apart variant exists for the march's native plain form (16, 32, 64 rows).
     const bool zg_trial = b->options.ops != WL_OPS_FIXED && b->set.plain();
+    // The staged variant exists for the three-phase blocks (1 row), where a tile takes it.
+    const bool stage_trial = b->set.staged_tiles() > 0u;
     for (uint32_t rows : {1u, 4u, 16u, 32u, 64u}) {
       for (uint32_t order : {0u, 1u}) {
-        for (uint32_t zg : {0u, 1u}) {
-          if (zg == 1u && !(zg_trial && rows >= 16u)) continue;
+        for (uint32_t v : {0u, 1u}) {
+          const uint32_t zg = rows >= 16u ? v : 0u, stage = rows == 1u ? v : 0u;
+          if (v == 1u && !(zg_trial && rows >= 16u) && !(stage_trial && rows == 1u)) continue;
           if (!b->set.reshape(shape_of_rows(rows), item_order(b->specs, order), &msg) ||
               !b->set.restore(&msg))
             return cuda_fail(err, err_len, msg);
           b->set.set_zero_apart(zg != 0u);
+          b->set.set_stage(stage != 0u ? wlc::TileSet::kStageOn : wlc::TileSet::kStageOff);
           // Each trial steps the same state past its first ticks untimed (a state as written is
           // often still: zero momenta, which flatter the zero-apart variant) and times the next
           // ones; every tuning steps to the same bytes, so each times the same ticks.
@@ -613,6 +624,7 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
             best.order = order;
             best.us_per_tick = us;
             best.zero_apart = zg;
+            best.stage = stage;
           }
         }
       }
@@ -624,6 +636,7 @@ int wl_batch_autotune(wl_batch* b, float max_dt, uint32_t trial_ticks, wl_tuning
   if (!b->set.reshape(shape_of_rows(best.block_rows), item_order(b->specs, best.order), &msg))
     return cuda_fail(err, err_len, msg);
   b->set.set_zero_apart(best.zero_apart != 0u);
+  b->set.set_stage(best.stage != 0u ? wlc::TileSet::kStageOn : wlc::TileSet::kStageOff);
   b->tuning = best;
   drop_graphs(b);
   if (chosen != nullptr) *chosen = best;

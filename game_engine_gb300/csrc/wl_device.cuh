@@ -86,6 +86,9 @@ struct TileDesc {
   float cell_m, gravity, cfl, dry;
   uint32_t blocks_x, blocks_y;  // work items: blocks of the launch's block shape
   uint32_t item_base, items;
+  // The block tick's tensor maps (three of 128 bytes: state copy 0's and copy 1's {h, hu, hv},
+  // then the bed), or null where the tile's rows do not start on 16-byte boundaries.
+  const void* tmap;
 };
 
 // A launch's dynamic work counter: CTAs take work items in order; the last CTA to leave resets it.
@@ -93,7 +96,7 @@ struct WorkCtl {
   uint32_t next;    // whole items dealt
   uint32_t exited;  // warps (or CTAs) that left
   uint32_t tail;    // the 32 x 16 march's last items dealt, a CTA at a time
-  uint32_t pad;
+  uint32_t fault;   // the staged block tick: nonzero where a CTA's wait on its copies gave up
 };
 
 // The resident tick's words (one a tile set, zeroed before each resident launch): the grid

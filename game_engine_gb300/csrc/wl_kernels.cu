@@ -30,13 +30,16 @@
 // Two other shapes share the items, the update (update_cell) and the last item's flip: the split
 // march (tick_split_kernel: a 32 x 16 item by a CTA's four warps, four rows each, for small tiles)
 // and the block tick (tick_block_kernel: a 32 x 16 item by 256 threads in three phases through
-// shared memory; the small-tile default and the stored-faces form). Every shape gives the same
-// bytes.
+// shared memory; the small-tile default and the stored-faces form; its staged variant takes a
+// block and its halo by two tensor copies). Every shape gives the same bytes.
 //
 // HBM traffic per cell-update: h, hu, hv, bed read (+ source, + Manning's n, + the remainder when
 // on), h, hu, hv written (+ the remainder), a 32-byte record per 256 cells.
 #include "wl_device.cuh"
 #include "wl_kernels.h"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 
@@ -931,7 +934,91 @@ struct BlockSmem {
   float ring[3 * 16 * kStrip];        // the cells' source, open-edge and roundoff volumes
   float fold[3 * kGroupCells];        // dt_main's fold (the tile's first block)
   uint32_t item, need, ab[4];
+  uint64_t bar;                       // the staged variant's copies land on this mbarrier
 };
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- the staged block: a block's cells and halo by tensor copies ------------------------------
+//
+// Where a tile's width is a multiple of 4 (its rows start on 16-byte boundaries), the block tick's
+// staged variant takes a 32 x 16 block's cells and one-cell halo as two tensor copies (TMA) into
+// shared memory, in place of each thread's global loads: the state's {h, hu, hv} as one box of
+// 40 x 18 x 3 floats and the bed as one of 40 x 18, both from column X0 - 4 and row Y0 - 1. X0 is
+// a multiple of 32, so every copy starts on a 16-byte boundary; the three columns west of the halo
+// are copied and not read. Cells past the tile's edges arrive as zeros and are not read either: a
+// ghost is its edge cell's reflection, which is in the box. The box lands in the faces' arrays,
+// which phase 1 does not use and phase 2 writes only after the CTA's barrier. One thread issues
+// both copies on the CTA's mbarrier; every thread waits on it, for at most kStageWaitNs.
+constexpr int kStageW = kBlkW + 8, kStageH = kBlkH + 2, kStageX = 4;
+constexpr int kStagePlane = kStageW * kStageH;                       // floats a plane
+constexpr uint32_t kStateBoxBytes = 3u * kStagePlane * 4u;           // 8640
+constexpr uint32_t kBedBoxBytes = uint32_t(kStagePlane) * 4u;        // 2880
+constexpr int kStageBed = int((kStateBoxBytes + 127u) / 128u * 32u);  // the bed box's float offset
+static_assert(kStageBed * 4 + kBedBoxBytes + 127 <=
+                  sizeof(float4) * (kBlkH * (kBlkW + 1) + (kBlkH + 1) * kBlkW),
+              "the stage fits in the faces' arrays");
+constexpr uint64_t kStageWaitNs = 1000000000ull;  // a second
+
+// The stage's first float: the faces' arrays' first 128-byte boundary.
+__device__ __forceinline__ float* stage_of(BlockSmem& m) {
+  char* p = reinterpret_cast<char*>(&m.fx[0][0]);
+  return reinterpret_cast<float*>(p + ((128u - (smem_u32(p) & 127u)) & 127u));
+}
+
+__device__ __forceinline__ void stage_init(BlockSmem& m) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&m.bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Thread 0: block (X0, Y0)'s boxes from state copy `cur` and the bed, on the mbarrier. The CTA
+// barrier before it ended every thread's use of the faces' arrays; the proxy fence orders those
+// generic writes before the copies' writes.
+__device__ __forceinline__ void stage_issue(BlockSmem& m, const TileDesc& T, uint32_t cur, int X0,
+                                            int Y0) {
+  const char* maps = static_cast<const char*>(T.tmap);
+  const uint32_t bar = smem_u32(&m.bar), dst = smem_u32(stage_of(m));
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+               "r"(kStateBoxBytes + kBedBoxBytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(maps + size_t(cur) * 128u), "r"(X0 - kStageX), "r"(Y0 - 1), "r"(0), "r"(bar)
+      : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst + uint32_t(kStageBed) * 4u),
+      "l"(maps + 256), "r"(X0 - kStageX), "r"(Y0 - 1), "r"(bar)
+      : "memory");
+}
+
+// Waits for phase `phase` of the mbarrier; false where it gave up after kStageWaitNs.
+__device__ __forceinline__ bool stage_wait(BlockSmem& m, uint32_t phase) {
+  const uint32_t bar = smem_u32(&m.bar);
+  uint64_t t0 = 0;
+  for (uint32_t k = 0;; ++k) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done != 0u) return true;
+    if (k == 0u) t0 = global_ns();
+    else if ((k & 15u) == 0u && global_ns() - t0 > kStageWaitNs) return false;
+  }
+}
 
 // The halo cell thread t reads (threads 0 .. 2 kBlkW + 2 kBlkH - 1; none for the others or past a
 // partial block's edge): its shared-memory slot, the cell it reads, and at the tile's edge the
@@ -939,6 +1026,7 @@ struct BlockSmem {
 struct HaloCell {
   float4* slot = nullptr;
   int i = 0;
+  int li = 0;  // the cell's float in a staged plane
   bool ghost = false, flip_v = false;
   float sign = 1.0f;
 };
@@ -985,6 +1073,7 @@ __device__ __forceinline__ HaloCell halo_cell(BlockSmem& m, int t, int X0, int Y
     h.slot = &m.cell[r + 1][cols + 1];
   }
   h.i = gy * nx + gx;
+  h.li = (gy - Y0 + 1) * kStageW + gx - X0 + kStageX;
   if (!need) h.slot = nullptr;
   return h;
 }
@@ -1008,12 +1097,15 @@ __device__ __forceinline__ void fold_ledger(const TileDesc& T, BlockSmem& m, uin
 // that holds the state, `rec` the record slot of the last update; pa and pb are the last update's
 // largest speeds; dt, whether the source applies and its scale are the tick's. Warp 0's lane 0
 // leaves the block's largest speeds in ia, ib for the caller, which counts the item. The tile's
-// first block folds its ledger unless a CTA of its own does (a.fold_apart).
-template <bool FIXED, bool MANNING, int THREADS>
-__device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, const TileDesc& T,
+// first block folds its ledger unless a CTA of its own does (a.fold_apart). STAGE: a tile with
+// tensor maps has its block's cells and halo copied into shared memory (phase `stage_phase` of the
+// CTA's mbarrier, flipped here); false (every thread alike) where the wait on the copies gave up,
+// the item not stepped and the launch's fault word marked.
+template <bool FIXED, bool MANNING, int THREADS, bool STAGE = false>
+__device__ __forceinline__ bool block_item(const TickArgs& a, BlockSmem& m, const TileDesc& T,
                                            uint32_t local, uint32_t cur, uint32_t rec, float pa,
                                            float pb, float dt, bool apply, float scale,
-                                           uint32_t& ia, uint32_t& ib) {
+                                           uint32_t& ia, uint32_t& ib, uint32_t& stage_phase) {
   constexpr int kBlkWarps = THREADS / 32;
   // The native arithmetic's zero arguments taken apart from its divisions and square roots (the
   // same bits): small tiles are mostly dry land, fronts and still water, where the intrinsics'
@@ -1022,6 +1114,8 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
   const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
+  const bool staged = STAGE && T.tmap != nullptr;
+  if (staged && t == 0) stage_issue(m, T, cur, X0, Y0);
   if (local == 0u && a.fold_apart == 0u) fold_ledger<FIXED>(T, m, rec, pa, pb, a.max_dt);
   const int nx = int(T.nx), ny = int(T.ny);
   const size_t n = size_t(T.nx) * T.ny;
@@ -1040,21 +1134,42 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
   constexpr bool kEarly = K == 1;
   float rh[K], rhu[K], rhv[K], rz[K], rsrc[K];
   bool live[K];
-  int gi[K];
+  int gi[K], si[K];
+  const float* st = staged ? stage_of(m) : nullptr;
+  bool failed = false;
+#pragma unroll
+  for (int k = 0; k < K; ++k) rsrc[k] = 0.0f;
+  if (staged) {
+    // The source's loads in flight while the copies land, then the wait.
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int r = warp + kBlkWarps * k;
+      if (K == 1 && apply && r < rows && cc < cols) rsrc[k] = T.source[(Y0 + r) * nx + X0 + cc];
+    }
+    failed = !stage_wait(m, stage_phase);
+  }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int r = warp + kBlkWarps * k;
     live[k] = r < rows && cc < cols;
     gi[k] = (Y0 + r) * nx + X0 + cc;
-    rh[k] = rhu[k] = rhv[k] = rz[k] = rsrc[k] = 0.0f;
+    si[k] = (r + 1) * kStageW + kStageX + cc;
+    rh[k] = rhu[k] = rhv[k] = rz[k] = 0.0f;
     if (live[k]) {
-      rh[k] = in[gi[k]];
-      rhu[k] = in[n + gi[k]];
-      rhv[k] = in[2 * n + gi[k]];
-      if (kEarly) rz[k] = bed[gi[k]];
-      // A thread of one cell loads its source with its state, not after the barriers (two
-      // cells' worth would cost the 256-thread CTA spills).
-      if (K == 1 && apply) rsrc[k] = T.source[gi[k]];
+      if (staged) {
+        rh[k] = st[si[k]];
+        rhu[k] = st[kStagePlane + si[k]];
+        rhv[k] = st[2 * kStagePlane + si[k]];
+        if (kEarly) rz[k] = st[kStageBed + si[k]];
+      } else {
+        rh[k] = in[gi[k]];
+        rhu[k] = in[n + gi[k]];
+        rhv[k] = in[2 * n + gi[k]];
+        if (kEarly) rz[k] = bed[gi[k]];
+        // A thread of one cell loads its source with its state, not after the barriers (two
+        // cells' worth would cost the 256-thread CTA spills).
+        if (K == 1 && apply) rsrc[k] = T.source[gi[k]];
+      }
     }
   }
   HaloCell hc;
@@ -1062,15 +1177,32 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
   if (kEarly) {
     hc = halo_cell(m, t, X0, Y0, rows, cols, nx, ny, flags);
     if (hc.slot != nullptr) {
-      qh = in[hc.i];
-      qhu = in[n + hc.i];
-      qhv = in[2 * n + hc.i];
-      qz = bed[hc.i];
+      if (staged) {
+        qh = st[hc.li];
+        qhu = st[kStagePlane + hc.li];
+        qhv = st[2 * kStagePlane + hc.li];
+        qz = st[kStageBed + hc.li];
+      } else {
+        qh = in[hc.i];
+        qhu = in[n + hc.i];
+        qhv = in[2 * n + hc.i];
+        qz = bed[hc.i];
+      }
     }
   }
+  // A staged wait that gave up (the whole CTA agrees): the launch's fault word, a last bounded
+  // wait for the copies still in flight into this CTA's shared memory, and the item not stepped.
+  auto give_up = [&]() {
+    if (t == 0) {
+      if (a.fault != nullptr) atomicOr(a.fault, 1u);
+      stage_wait(m, stage_phase);
+    }
+    return false;
+  };
   uint32_t ga = 0u, gb = 0u;
   bool opn_seen = false, rnd_seen = false;
   if (!(dt > 0.0f)) {
+    if (staged && __syncthreads_or(failed)) return give_up();
     // A step of no length: the state as it is, to the bit (slang:576-585).
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -1091,15 +1223,23 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
 #pragma unroll
     for (int k = 0; k < K; ++k)
       if (live[k])
-        m.cell[warp + kBlkWarps * k + 1][cc + 1] =
-            velocities<FIXED, kZeroApart>(rh[k], rhu[k], rhv[k], kEarly ? rz[k] : bed[gi[k]], dry);
+        m.cell[warp + kBlkWarps * k + 1][cc + 1] = velocities<FIXED, kZeroApart>(
+            rh[k], rhu[k], rhv[k],
+            kEarly ? rz[k] : (staged ? st[kStageBed + si[k]] : bed[gi[k]]), dry);
     if (!kEarly) {
       hc = halo_cell(m, t, X0, Y0, rows, cols, nx, ny, flags);
       if (hc.slot != nullptr) {
-        qh = in[hc.i];
-        qhu = in[n + hc.i];
-        qhv = in[2 * n + hc.i];
-        qz = bed[hc.i];
+        if (staged) {
+          qh = st[hc.li];
+          qhu = st[kStagePlane + hc.li];
+          qhv = st[2 * kStagePlane + hc.li];
+          qz = st[kStageBed + hc.li];
+        } else {
+          qh = in[hc.i];
+          qhu = in[n + hc.i];
+          qhv = in[2 * n + hc.i];
+          qz = bed[hc.i];
+        }
       }
     }
     if (hc.slot != nullptr) {
@@ -1110,7 +1250,12 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
       }
       *hc.slot = v;
     }
-    __syncthreads();
+    // The stage's last reads end here: phase 2 writes the faces over it.
+    if (STAGE) {
+      if (__syncthreads_or(failed)) return give_up();
+    } else {
+      __syncthreads();
+    }
     // 2. the faces
     const int nfx = rows * (cols + 1), nfy = (rows + 1) * cols;
     const bool full = cols == kBlkW;
@@ -1188,9 +1333,13 @@ __device__ __forceinline__ void block_item(const TickArgs& a, BlockSmem& m, cons
                   m.ab[lane < 16 ? 1 : 3], m.ring, dt > 0.0f && apply, (need & 1u) != 0u,
                   (need & 2u) != 0u, ia, ib);
   }
+  if (staged) stage_phase ^= 1u;
+  return true;
 }
 
-template <bool FIXED, bool MANNING, int THREADS>
+// STAGE: the staged variant (a tile with tensor maps takes its blocks by tensor copies; the
+// others load cell by cell).
+template <bool FIXED, bool MANNING, int THREADS, bool STAGE = false>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(TickArgs a) {
   static_assert(THREADS >= int(kGroupCells) && THREADS % 32 == 0,
                 "fold_block takes a thread a virtual lane");
@@ -1201,6 +1350,14 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
   if (threadIdx.x == 0 && blockIdx.x < a.n_items) {
     const TileDesc* d = a.tiles + item_tile_of(a.item_tile, blockIdx.x);
     asm volatile("prefetch.global.L1 [%0];" ::"l"(d));
+    // The staged variant: the first item's three tensor maps into the copy engine's cache (they,
+    // too, only change with the host's uploads), so its copies need no fetch of their own.
+    if (STAGE) {
+      const char* maps = static_cast<const char*>(d->tmap);
+      if (maps != nullptr)
+        for (int k = 0; k < 3; ++k)
+          asm volatile("prefetch.tensormap [%0];" ::"l"(maps + 128 * k) : "memory");
+    }
   }
   dependent_grid_start();
   if (a.go != nullptr && *a.go == 0u) return;
@@ -1220,6 +1377,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     if (t == 0) finish_item(T, rec, 0u, 0u, true, 1u);
     return;
   }
+  uint32_t stage_phase = 0u;
+  if (STAGE && t == 0) stage_init(m);  // ordered before any wait by the loop's first barrier
   for (bool first = true;; first = false) {
     if (t == 0) {
       m.item = take_item(a.work, first, blockIdx.x, gridDim.x, a.n_items);
@@ -1245,8 +1404,9 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const bool apply = src_flag && (T.source_every <= 1u || ctl->src_phase + 1u == T.source_every);
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
     uint32_t ia = 0u, ib = 0u;
-    block_item<FIXED, MANNING, THREADS>(a, m, T, local, cur, rec, pa, pb, dt, apply, scale, ia,
-                                        ib);
+    if (!block_item<FIXED, MANNING, THREADS, STAGE>(a, m, T, local, cur, rec, pa, pb, dt, apply,
+                                                    scale, ia, ib, stage_phase))
+      break;  // a staged wait gave up: the fault word is marked
     if (t == 0) finish_item(T, rec, ia, ib, true, a.fold_apart);
     __syncthreads();
   }
@@ -1287,12 +1447,6 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
 // word and the CTA leaves, and so does every CTA that then sees the mark, so the launch ends; the
 // host reads the word.
 constexpr uint64_t kResidentWaitNs = 1000000000ull;  // a second
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 // The barrier in two halves, so that a CTA works while it waits: `resident_arrive` (after a CTA
 // barrier: every thread's writes of the tick are done) adds the CTA's arrival with release
@@ -1862,12 +2016,18 @@ const void* block_fn(bool fixed, bool manning) {
                  : (const void*)tick_block_kernel<false, false, THREADS>;
 }
 
+template <int THREADS, bool STAGE>
+void (*block_kernel(bool fixed, bool manning))(TickArgs) {
+  return fixed ? (manning ? tick_block_kernel<true, true, THREADS, STAGE>
+                          : tick_block_kernel<true, false, THREADS, STAGE>)
+               : (manning ? tick_block_kernel<false, true, THREADS, STAGE>
+                          : tick_block_kernel<false, false, THREADS, STAGE>);
+}
+
 template <int THREADS>
 cudaError_t block_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
-  void (*k)(TickArgs) =
-      fixed ? (manning ? tick_block_kernel<true, true, THREADS> : tick_block_kernel<true, false, THREADS>)
-            : (manning ? tick_block_kernel<false, true, THREADS>
-                       : tick_block_kernel<false, false, THREADS>);
+  void (*k)(TickArgs) = a.stage != 0u ? block_kernel<THREADS, true>(fixed, manning)
+                                      : block_kernel<THREADS, false>(fixed, manning);
   return launch_dependent(k, dim3(grid), dim3(THREADS), sizeof(BlockSmem), s, a);
 }
 
@@ -1939,6 +2099,43 @@ cudaError_t launch_settled(const TileDesc* tiles, uint32_t tile0, uint32_t count
         tiles, tile0 + k, first, h, hu, hv, dev + 2 * size_t(k));
   }
   return cudaGetLastError();
+}
+
+bool encode_stage_maps(const TileDesc& d, void* maps) {
+  static_assert(sizeof(CUtensorMap) == 128, "a tensor map is 128 bytes");
+  // The driver's encoder, looked up once through the runtime (no link against the driver).
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  // A box's x must start on a 16-byte boundary: rows of a multiple of 4 floats, and X0 - 4 with X0
+  // a multiple of 32. The planes' strides (row: 4 nx bytes, plane: 4 nx ny) are then multiples of
+  // 16, as a tensor map requires, and every allocation the kernels read starts on 256 bytes.
+  if (encode == nullptr || d.nx % 4u != 0u || d.nx == 0u || d.ny == 0u) return false;
+  CUtensorMap* m = static_cast<CUtensorMap*>(maps);
+  const cuuint64_t n = cuuint64_t(d.nx) * d.ny;
+  const cuuint32_t unit[3] = {1, 1, 1};
+  for (int c = 0; c < 2; ++c) {
+    const cuuint64_t dims[3] = {d.nx, d.ny, 3};
+    const cuuint64_t strides[2] = {cuuint64_t(d.nx) * 4u, n * 4u};
+    const cuuint32_t box[3] = {kStageW, kStageH, 3};
+    if (encode(&m[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, d.state[c], dims, strides, box, unit,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  const cuuint64_t dims[2] = {d.nx, d.ny};
+  const cuuint64_t strides[1] = {cuuint64_t(d.nx) * 4u};
+  const cuuint32_t box[2] = {kStageW, kStageH};
+  return encode(&m[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(d.bed), dims,
+                strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
 }
 
 size_t tick_smem_bytes(BlockShape shape) {

@@ -30,6 +30,11 @@ struct TickArgs {
   // The march's native plain variant with zero arguments taken apart from its divisions and
   // square roots (the same bits; faster where many arguments are zero, slower where few are).
   uint32_t zero_apart = 0;
+  // The block shapes' staged variant: a block's cells and halo taken by two tensor copies into
+  // shared memory (tiles with tensor maps; the others load cell by cell). `fault` is the word a
+  // CTA marks where its wait on the copies gave up.
+  uint32_t stage = 0;
+  uint32_t* fault = nullptr;
 };
 
 // The block of cells one work item steps: 32 columns by 16, 32 or 64 rows, one warp marching
@@ -52,6 +57,10 @@ int tick_occupancy(BlockShape shape, bool fixed, bool manning, bool plain);
 
 cudaError_t launch_tick(BlockShape shape, bool fixed, bool manning, bool plain, const TickArgs& a,
                         int grid, cudaStream_t s);
+// The staged block tick's three tensor maps of tile `d` (its state pointers and sizes set) into
+// `maps` (384 bytes, 64-byte aligned, host memory): false, and no maps, where its width is not a
+// multiple of 4 (rows off 16-byte boundaries) or the driver offers no tensor-map encoder.
+bool encode_stage_maps(const TileDesc& d, void* maps);
 // The records of the states just written (one CTA a work item, the same items as the tick's).
 // The resident tick: `ticks` ticks of tile 0 (the wide block tick's items) in one cooperative
 // launch of a.n_items + 1 CTAs, a grid barrier between ticks. `rc` (zeroed here, on `s`, before

@@ -49,7 +49,7 @@ __global__ void static_init_kernel(StaticScratch* s, TileDesc d) {
   s->work.next = 0u;
   s->work.exited = 0u;
   s->work.tail = 0u;
-  s->work.pad = 0u;
+  s->work.fault = 0u;
 }
 
 std::mutex g_mu;

@@ -14,6 +14,7 @@ namespace wlc {
 namespace {
 
 constexpr size_t kAlign = 256;
+constexpr size_t kMapBytes = 128;  // a tensor map
 
 size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
@@ -167,6 +168,9 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
   total += align_up((1 + nt) * sizeof(WorkCtl));
   const size_t off_res = total;
   total += align_up(sizeof(ResidentCtl));
+  // The staged block tick's tensor maps, three of 128 bytes a tile.
+  const size_t off_maps = total;
+  total += align_up(nt * 3 * kMapBytes);
   if (!check(cudaMalloc(&base_, total), err, "cudaMalloc")) {
     base_ = nullptr;
     destroy();
@@ -217,6 +221,27 @@ bool TileSet::create(int device, const std::vector<TileSpec>& tiles, bool fixed_
     d.gravity = static_cast<float>(t.gravity);
     d.cfl = static_cast<float>(t.cfl);
     d.dry = static_cast<float>(t.dry_depth_m);
+  }
+  // The tensor maps of every tile whose shape allows them (encoded here, uploaded once: they
+  // describe the tile's fixed allocations).
+  {
+    std::vector<unsigned char> maps(nt * 3 * kMapBytes + 64);
+    unsigned char* h = maps.data() + ((64u - reinterpret_cast<uintptr_t>(maps.data()) % 64u) % 64u);
+    char* dev = base_ + off_maps;
+    staged_tiles_ = 0;
+    for (size_t i = 0; i < nt; ++i) {
+      TileDesc& d = host_[i];
+      d.tmap = nullptr;
+      if (encode_stage_maps(d, h + i * 3 * kMapBytes)) {
+        d.tmap = dev + i * 3 * kMapBytes;
+        ++staged_tiles_;
+      }
+    }
+    if (!check(cudaMemcpyAsync(dev, h, nt * 3 * kMapBytes, cudaMemcpyHostToDevice, stream_), err,
+               "upload of the tensor maps")) {
+      destroy();
+      return false;
+    }
   }
   // Empty ledgers: every field zero but the time left, +inf between advances.
   std::vector<TileCtl> ctl(nt);
@@ -339,11 +364,13 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   a.max_dt = max_dt;
   a.go = go;
   a.zero_apart = zero_apart_ ? 1u : 0u;
+  a.fault = &d_work_->fault;
   const bool manning = any_manning(), plain_set = plain();
   // The block shape's wide CTA where the launch holds no more blocks than the device has SMs; for
   // one tile, one CTA more folds its ledger beside the items.
   const bool wide = shape_ == BlockShape::k32x16b && n_items_ <= uint32_t(sms_);
   const BlockShape shape = wide ? BlockShape::k32x16w : shape_;
+  a.stage = stages(shape) ? 1u : 0u;
   int grid = grid_;
   if (wide && d_item_tile_ == nullptr) {
     a.fold_apart = 1u;
@@ -356,6 +383,7 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
       }
     }
   }
+  if (a.stage != 0u) stage_used_ = true;
   for (uint32_t i = 0; i < count; ++i) {
     const cudaError_t e = launch_tick(shape, fixed_, manning, plain_set, a, grid, s);
     if (e != cudaSuccess) return e;
@@ -372,6 +400,9 @@ cudaError_t TileSet::enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_
   a.n_items = host_[tile].items;
   a.max_dt = max_dt;
   a.zero_apart = zero_apart_ ? 1u : 0u;
+  a.stage = stages(shape_) && host_[tile].tmap != nullptr ? 1u : 0u;
+  a.fault = &d_work_->fault;
+  if (a.stage != 0u) stage_used_ = true;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
   const bool manning = (host_[tile].flags & kFlagManning) != 0u;
@@ -429,6 +460,19 @@ bool TileSet::wait(std::string* err) {
       return false;
     if (word != 0u) {
       if (err) *err = "water_live: the resident tick's grid barrier gave up (a CTA did not arrive)";
+      return false;
+    }
+  }
+  if (stage_used_) {
+    // A staged block launch marks the fault word where a CTA's wait on its copies gave up; the
+    // state is then not the ticks' result.
+    stage_used_ = false;
+    uint32_t word = 0u;
+    if (!check(cudaMemcpy(&word, &d_work_->fault, sizeof word, cudaMemcpyDeviceToHost), err,
+               "read-back of the staged tick's fault word"))
+      return false;
+    if (word != 0u) {
+      if (err) *err = "water_live: the staged block tick's copies did not land (wait gave up)";
       return false;
     }
   }

@@ -50,6 +50,27 @@ class TileSet {
   // knob). The same bits either way.
   void set_zero_apart(bool on) { zero_apart_ = on; }
   bool zero_apart() const { return zero_apart_; }
+  // The block shapes' staged variant (TickArgs::stage): a tile whose width is a multiple of 4
+  // takes each block's cells and halo by tensor copies. The same bits either way. kStageOff,
+  // kStageOn (both block CTAs), or kStageAuto: the 256-thread CTA only, whose threads would
+  // otherwise load a block in two rounds (cells, then bed and halo), where the 512-thread CTA's
+  // one round is shorter than the copies' latency (256 x 256 a launch a tick: 7.2 against 7.5 us;
+  // 512 x 512: 11.8 against 11.7).
+  static constexpr uint32_t kStageOff = 0, kStageOn = 1, kStageAuto = 2;
+  void set_stage(uint32_t mode) { stage_ = mode; }
+  uint32_t stage() const { return stage_; }
+  // Tiles with tensor maps (the staged variant's tiles), and those the set's launches stage.
+  uint32_t staged_tiles() const { return staged_tiles_; }
+  uint32_t staged_launch_tiles() const {
+    if (shape_ != BlockShape::k32x16b) return 0u;
+    return stages(n_items_ <= uint32_t(sms_) ? BlockShape::k32x16w : shape_) ? staged_tiles_ : 0u;
+  }
+  bool stages(BlockShape launch) const {
+    return staged_tiles_ > 0u &&
+           ((stage_ == kStageOn &&
+             (launch == BlockShape::k32x16b || launch == BlockShape::k32x16w)) ||
+            (stage_ == kStageAuto && launch == BlockShape::k32x16b));
+  }
   // One tile's own tick (the per-tile-launch form): only that tile's work items.
   cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);
   cudaError_t enqueue_prime(cudaStream_t s);
@@ -135,6 +156,9 @@ class TileSet {
   bool resident_used_ = false;      // a resident launch since the last wait()
   uint64_t tick_launches_ = 0;
   bool zero_apart_ = false;
+  uint32_t stage_ = kStageOff;
+  bool stage_used_ = false;  // a staged block launch since the last wait()
+  uint32_t staged_tiles_ = 0;
   uint32_t* d_item_tile_ = nullptr;  // the tile of each work item (null for one tile)
   uint32_t n_items_ = 0;
   int grid_ = 0;

@@ -209,6 +209,11 @@ class DeviceStep:
         call's ticks in one resident launch, a larger one a launch a tick."""
         return int(lib().wl_tick_launches(self._h)) if self._h is not None else 0
 
+    def staged_tiles(self) -> int:
+        """1 where the step's three-phase blocks take their cells and halo by tensor copies (a
+        width that is a multiple of 4, and 256-thread CTAs or WLCUDA_STAGE=1 at create), else 0."""
+        return int(lib().wl_staged_tiles(self._h)) if self._h is not None else 0
+
     def run_steps(self, count: int, max_dt: float) -> bool:
         return self._ok(lib().wl_run_steps(self._h, int(count), float(max_dt), self._buf,
                                            len(self._buf)))

@@ -126,6 +126,11 @@ uint32_t wl_group_count(const wl_step* step);
  * counter). A tile of no more 32 x 16 blocks than the device holds resident CTAs steps a call's two
  * or more ticks in one launch; other tiles take a launch a tick. 0 for an invalid handle. */
 uint64_t wl_tick_launches(const wl_step* step);
+/* Tiles whose 32 x 16 blocks the step's launches take by tensor copies (no counterpart in the
+ * reference: a diagnosis count): 1 where the tile's width is a multiple of 4 and the step ticks in
+ * three-phase blocks of 256-thread CTAs (more blocks than SMs), or in either block CTA with
+ * WLCUDA_STAGE=1 set at create (WLCUDA_STAGE=0: in neither); else 0. */
+uint32_t wl_staged_tiles(const wl_step* step);
 
 /* DeviceStep::write_state (water_live.cpp:271-314): each array n = nx * ny doubles, rounded to
  * float; plane 3 zeroed; the ledger emptied; the source clock restarted. */
@@ -225,12 +230,16 @@ typedef struct wl_tile {
  * open edge, no compensated source): 1 takes a zero argument of the march's divisions and square
  * roots apart from the IEEE intrinsic (sqrt(+-0) = +-0, 0 / b = +-0 for b > 0), the same bits
  * without the intrinsic's slow path: faster where many arguments are zero (dry land, wet/dry
- * fronts, still columns), slower where few are; the autotuner tries both. */
+ * fronts, still columns), slower where few are; the autotuner tries both. stage (block_rows 1):
+ * 1 takes each 32 x 16 block's cells and halo into shared memory by two tensor copies (TMA) in
+ * place of each thread's loads, for tiles whose width is a multiple of 4 (the others load cell by
+ * cell); the same bits either way. */
 typedef struct wl_tuning {
   uint32_t block_rows;
   uint32_t order;
   float us_per_tick;
   uint32_t zero_apart;
+  uint32_t stage;
 } wl_tuning;
 
 /* `common` gives cell_m, gravity, cfl, dry_depth_m and device (its nx, ny and edges are unused). */
@@ -239,6 +248,9 @@ int wl_batch_create(const wl_config* common, const wl_options* options, const wl
 void wl_batch_destroy(wl_batch* batch);
 uint32_t wl_batch_tile_count(const wl_batch* batch);
 uint64_t wl_batch_cell_count(const wl_batch* batch);
+/* Tiles whose 32 x 16 blocks the batch's launches take by tensor copies under its tuning (block_rows
+ * 1 and stage 1: the tiles whose width is a multiple of 4; else 0). A diagnosis count. */
+uint32_t wl_batch_staged_tiles(const wl_batch* batch);
 uint64_t wl_batch_tile_first(const wl_batch* batch, uint32_t tile);
 
 /* write_state / set_bed / set_manning / set_source of every tile at once (total = all cells). */
