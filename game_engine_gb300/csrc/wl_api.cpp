@@ -143,8 +143,8 @@ int wl_create(const wl_config* config, const wl_options* options, wl_step** out,
     return cuda_fail(err, err_len, msg);
   }
   // The block shape's staged variant (a block's cells and halo by tensor copies, where the tile's
-  // width is a multiple of 4): by default in the 256-thread block CTA only; WLCUDA_STAGE=1 in both
-  // block CTAs, 0 in neither. The same bytes either way.
+  // width is a multiple of 4): by default where a launch of 256-thread block CTAs holds more blocks
+  // than CTAs; WLCUDA_STAGE=1 in every block launch, 0 in none. The same bytes either way.
   s->set.set_stage(wlc::TileSet::kStageAuto);
   if (const char* stage = std::getenv("WLCUDA_STAGE")) {
     if (std::strcmp(stage, "0") == 0) s->set.set_stage(wlc::TileSet::kStageOff);

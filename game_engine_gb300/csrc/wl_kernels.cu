@@ -934,6 +934,9 @@ struct BlockSmem {
   float ring[3 * 16 * kStrip];        // the cells' source, open-edge and roundoff volumes
   float fold[3 * kGroupCells];        // dt_main's fold (the tile's first block)
   uint32_t item, need, ab[4];
+  // The staged variant: whether copies are in flight for `item`, and the next item (taken while
+  // this one steps) with whether its copies were issued.
+  uint32_t staged, next, next_staged;
   uint64_t bar;                       // the staged variant's copies land on this mbarrier
 };
 
@@ -955,22 +958,28 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 // 40 x 18 x 3 floats and the bed as one of 40 x 18, both from column X0 - 4 and row Y0 - 1. X0 is
 // a multiple of 32, so every copy starts on a 16-byte boundary; the three columns west of the halo
 // are copied and not read. Cells past the tile's edges arrive as zeros and are not read either: a
-// ghost is its edge cell's reflection, which is in the box. The box lands in the faces' arrays,
-// which phase 1 does not use and phase 2 writes only after the CTA's barrier. One thread issues
-// both copies on the CTA's mbarrier; every thread waits on it, for at most kStageWaitNs.
+// ghost is its edge cell's reflection, which is in the box. The box has a shared-memory region of
+// its own after the CTA's BlockSmem. One thread issues both copies on the CTA's mbarrier; every
+// thread waits on it, for at most kStageWaitNs.
+//
+// A CTA that steps block after block takes its next block while it steps this one: thread 0 takes
+// the next item from the work counter at the item's start, and issues its copies as soon as this
+// block's last read of the stage is behind a CTA barrier (phase 1's), so that they land while the
+// CTA computes this block's faces and updates.
 constexpr int kStageW = kBlkW + 8, kStageH = kBlkH + 2, kStageX = 4;
 constexpr int kStagePlane = kStageW * kStageH;                       // floats a plane
 constexpr uint32_t kStateBoxBytes = 3u * kStagePlane * 4u;           // 8640
 constexpr uint32_t kBedBoxBytes = uint32_t(kStagePlane) * 4u;        // 2880
 constexpr int kStageBed = int((kStateBoxBytes + 127u) / 128u * 32u);  // the bed box's float offset
-static_assert(kStageBed * 4 + kBedBoxBytes + 127 <=
-                  sizeof(float4) * (kBlkH * (kBlkW + 1) + (kBlkH + 1) * kBlkW),
-              "the stage fits in the faces' arrays");
+constexpr size_t kStageBytes = size_t(kStageBed) * 4u + kBedBoxBytes;  // 11584
+// The staged kernel's dynamic shared memory: BlockSmem, up to 127 bytes to the next 128-byte
+// boundary, the stage.
+constexpr size_t kStagedSmemBytes = sizeof(BlockSmem) + 128u + kStageBytes;
 constexpr uint64_t kStageWaitNs = 1000000000ull;  // a second
 
-// The stage's first float: the faces' arrays' first 128-byte boundary.
+// The stage's first float: the first 128-byte boundary past the CTA's BlockSmem.
 __device__ __forceinline__ float* stage_of(BlockSmem& m) {
-  char* p = reinterpret_cast<char*>(&m.fx[0][0]);
+  char* p = reinterpret_cast<char*>(&m) + sizeof(BlockSmem);
   return reinterpret_cast<float*>(p + ((128u - (smem_u32(p) & 127u)) & 127u));
 }
 
@@ -979,9 +988,9 @@ __device__ __forceinline__ void stage_init(BlockSmem& m) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Thread 0: block (X0, Y0)'s boxes from state copy `cur` and the bed, on the mbarrier. The CTA
-// barrier before it ended every thread's use of the faces' arrays; the proxy fence orders those
-// generic writes before the copies' writes.
+// Thread 0: block (X0, Y0)'s boxes from state copy `cur` and the bed, on the mbarrier. A CTA
+// barrier before it ended every thread's reads of the stage; the proxy fence orders the CTA's
+// generic accesses before the copies' writes.
 __device__ __forceinline__ void stage_issue(BlockSmem& m, const TileDesc& T, uint32_t cur, int X0,
                                             int Y0) {
   const char* maps = static_cast<const char*>(T.tmap);
@@ -1018,6 +1027,21 @@ __device__ __forceinline__ bool stage_wait(BlockSmem& m, uint32_t phase) {
     if (k == 0u) t0 = global_ns();
     else if ((k & 15u) == 0u && global_ns() - t0 > kStageWaitNs) return false;
   }
+}
+
+// Thread 0: issues item `item`'s copies where it has any (an item of the launch, of a tile with
+// tensor maps, not a landed tile's in a queue's launch); returns whether it did. The item's tile
+// cannot flip its copy before the item is stepped, so `cur` read now is the item's.
+__device__ __forceinline__ uint32_t stage_item(const TickArgs& a, BlockSmem& m, uint32_t item) {
+  if (item >= a.n_items) return 0u;
+  const TileDesc& T = a.tiles[item_tile_of(a.item_tile, item)];
+  if (T.tmap == nullptr) return 0u;
+  const TileCtl* ctl = T.ctl;
+  if (a.go != nullptr && !(ctl->ledger[ctl->rec].remaining_s > 0.0f)) return 0u;
+  const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
+  const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
+  stage_issue(m, T, ctl->cur, int(bx) * kBlkW, int(by) * kBlkH);
+  return 1u;
 }
 
 // The halo cell thread t reads (threads 0 .. 2 kBlkW + 2 kBlkH - 1; none for the others or past a
@@ -1097,15 +1121,18 @@ __device__ __forceinline__ void fold_ledger(const TileDesc& T, BlockSmem& m, uin
 // that holds the state, `rec` the record slot of the last update; pa and pb are the last update's
 // largest speeds; dt, whether the source applies and its scale are the tick's. Warp 0's lane 0
 // leaves the block's largest speeds in ia, ib for the caller, which counts the item. The tile's
-// first block folds its ledger unless a CTA of its own does (a.fold_apart). STAGE: a tile with
-// tensor maps has its block's cells and halo copied into shared memory (phase `stage_phase` of the
-// CTA's mbarrier, flipped here); false (every thread alike) where the wait on the copies gave up,
-// the item not stepped and the launch's fault word marked.
-template <bool FIXED, bool MANNING, int THREADS, bool STAGE = false>
+// first block folds its ledger unless a CTA of its own does (a.fold_apart). STAGE: `staged` says
+// the block's cells and halo are being copied into the stage (phase `stage_phase` of the CTA's
+// mbarrier, flipped here); `after_reads` runs once every thread's reads of the stage are behind a
+// CTA barrier (the caller issues the next block's copies there). Returns false (every thread
+// alike) where the wait on the copies gave up: the item not stepped, the launch's fault word
+// marked.
+template <bool FIXED, bool MANNING, int THREADS, bool STAGE = false, class AfterReads>
 __device__ __forceinline__ bool block_item(const TickArgs& a, BlockSmem& m, const TileDesc& T,
                                            uint32_t local, uint32_t cur, uint32_t rec, float pa,
                                            float pb, float dt, bool apply, float scale,
-                                           uint32_t& ia, uint32_t& ib, uint32_t& stage_phase) {
+                                           uint32_t& ia, uint32_t& ib, bool staged,
+                                           uint32_t& stage_phase, AfterReads after_reads) {
   constexpr int kBlkWarps = THREADS / 32;
   // The native arithmetic's zero arguments taken apart from its divisions and square roots (the
   // same bits): small tiles are mostly dry land, fronts and still water, where the intrinsics'
@@ -1114,8 +1141,7 @@ __device__ __forceinline__ bool block_item(const TickArgs& a, BlockSmem& m, cons
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const uint32_t by = local / T.blocks_x, bx = local - by * T.blocks_x;
   const int X0 = int(bx) * kBlkW, Y0 = int(by) * kBlkH;
-  const bool staged = STAGE && T.tmap != nullptr;
-  if (staged && t == 0) stage_issue(m, T, cur, X0, Y0);
+  staged = STAGE && staged;
   if (local == 0u && a.fold_apart == 0u) fold_ledger<FIXED>(T, m, rec, pa, pb, a.max_dt);
   const int nx = int(T.nx), ny = int(T.ny);
   const size_t n = size_t(T.nx) * T.ny;
@@ -1203,6 +1229,7 @@ __device__ __forceinline__ bool block_item(const TickArgs& a, BlockSmem& m, cons
   bool opn_seen = false, rnd_seen = false;
   if (!(dt > 0.0f)) {
     if (staged && __syncthreads_or(failed)) return give_up();
+    after_reads();
     // A step of no length: the state as it is, to the bit (slang:576-585).
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -1250,9 +1277,10 @@ __device__ __forceinline__ bool block_item(const TickArgs& a, BlockSmem& m, cons
       }
       *hc.slot = v;
     }
-    // The stage's last reads end here: phase 2 writes the faces over it.
+    // The stage's last reads end here.
     if (STAGE) {
       if (__syncthreads_or(failed)) return give_up();
+      after_reads();
     } else {
       __syncthreads();
     }
@@ -1381,13 +1409,29 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
   if (STAGE && t == 0) stage_init(m);  // ordered before any wait by the loop's first barrier
   for (bool first = true;; first = false) {
     if (t == 0) {
-      m.item = take_item(a.work, first, blockIdx.x, gridDim.x, a.n_items);
+      if (!STAGE || first) {
+        m.item = take_item(a.work, first, blockIdx.x, gridDim.x, a.n_items);
+        if (STAGE) m.staged = stage_item(a, m, m.item);
+      } else {
+        m.item = m.next;  // taken, and its copies issued, while the last item stepped
+        m.staged = m.next_staged;
+      }
       m.need = 0u;
     }
     if (t < 4) m.ab[t] = 0u;
     __syncthreads();
     const uint32_t item = m.item;
     if (item >= a.n_items) break;
+    // STAGE: the next item is taken now (the counter's round trip runs behind this item's first
+    // phase), and its copies are issued once this block's reads of the stage are done.
+    uint32_t next = 0u;
+    if (STAGE && t == 0) next = take_item(a.work, false, blockIdx.x, gridDim.x, a.n_items);
+    auto after_reads = [&]() {
+      if (STAGE && t == 0) {
+        m.next = next;
+        m.next_staged = stage_item(a, m, next);
+      }
+    };
     const uint32_t tile = item_tile_of(a.item_tile, item);
     const TileDesc& T = a.tiles[tile];
     const uint32_t local = a.item_tile == nullptr ? item : item - T.item_base;
@@ -1397,6 +1441,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const float dt =
         choose_dt<FIXED>(pa, pb, T.cfl, T.cell_m, a.max_dt, ctl->ledger[rec].remaining_s);
     if (a.go != nullptr && !(ctl->ledger[rec].remaining_s > 0.0f)) {  // a landed tile
+      after_reads();  // no copies were issued for it: the stage is free
       __syncthreads();
       continue;
     }
@@ -1405,7 +1450,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) tick_block_kernel(Tic
     const float scale = T.source_every > 1u ? float(T.source_every) : 1.0f;
     uint32_t ia = 0u, ib = 0u;
     if (!block_item<FIXED, MANNING, THREADS, STAGE>(a, m, T, local, cur, rec, pa, pb, dt, apply,
-                                                    scale, ia, ib, stage_phase))
+                                                    scale, ia, ib, STAGE && m.staged != 0u,
+                                                    stage_phase, after_reads))
       break;  // a staged wait gave up: the fault word is marked
     if (t == 0) finish_item(T, rec, ia, ib, true, a.fold_apart);
     __syncthreads();
@@ -2026,9 +2072,12 @@ void (*block_kernel(bool fixed, bool manning))(TickArgs) {
 
 template <int THREADS>
 cudaError_t block_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {
-  void (*k)(TickArgs) = a.stage != 0u ? block_kernel<THREADS, true>(fixed, manning)
-                                      : block_kernel<THREADS, false>(fixed, manning);
-  return launch_dependent(k, dim3(grid), dim3(THREADS), sizeof(BlockSmem), s, a);
+  static_assert(kStagedSmemBytes <= 48u * 1024u, "the staged block tick needs no opt-in");
+  if (a.stage != 0u)
+    return launch_dependent(block_kernel<THREADS, true>(fixed, manning), dim3(grid),
+                            dim3(THREADS), kStagedSmemBytes, s, a);
+  return launch_dependent(block_kernel<THREADS, false>(fixed, manning), dim3(grid), dim3(THREADS),
+                          sizeof(BlockSmem), s, a);
 }
 
 cudaError_t split_launch(bool fixed, bool manning, const TickArgs& a, int grid, cudaStream_t s) {

@@ -370,7 +370,6 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
   // one tile, one CTA more folds its ledger beside the items.
   const bool wide = shape_ == BlockShape::k32x16b && n_items_ <= uint32_t(sms_);
   const BlockShape shape = wide ? BlockShape::k32x16w : shape_;
-  a.stage = stages(shape) ? 1u : 0u;
   int grid = grid_;
   if (wide && d_item_tile_ == nullptr) {
     a.fold_apart = 1u;
@@ -383,6 +382,7 @@ cudaError_t TileSet::enqueue_ticks(cudaStream_t s, uint32_t count, float max_dt,
       }
     }
   }
+  a.stage = stages(shape, n_items_, grid) ? 1u : 0u;
   if (a.stage != 0u) stage_used_ = true;
   for (uint32_t i = 0; i < count; ++i) {
     const cudaError_t e = launch_tick(shape, fixed_, manning, plain_set, a, grid, s);
@@ -400,15 +400,15 @@ cudaError_t TileSet::enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_
   a.n_items = host_[tile].items;
   a.max_dt = max_dt;
   a.zero_apart = zero_apart_ ? 1u : 0u;
-  a.stage = stages(shape_) && host_[tile].tmap != nullptr ? 1u : 0u;
   a.fault = &d_work_->fault;
-  if (a.stage != 0u) stage_used_ = true;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
   const bool manning = (host_[tile].flags & kFlagManning) != 0u;
   const bool plain_tile = (host_[tile].flags & kFlagsNotPlain) == 0u;
   const int occ = std::max(1, tick_occupancy(shape_, fixed_, manning, plain_tile));
   const int grid = std::max(1, std::min<int>(int(a.n_items), sms * occ));
+  a.stage = stages(shape_, a.n_items, grid) && host_[tile].tmap != nullptr ? 1u : 0u;
+  if (a.stage != 0u) stage_used_ = true;
   return launch_tick(shape_, fixed_, manning, plain_tile, a, grid, s);
 }
 

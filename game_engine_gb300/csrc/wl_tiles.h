@@ -51,11 +51,12 @@ class TileSet {
   void set_zero_apart(bool on) { zero_apart_ = on; }
   bool zero_apart() const { return zero_apart_; }
   // The block shapes' staged variant (TickArgs::stage): a tile whose width is a multiple of 4
-  // takes each block's cells and halo by tensor copies. The same bits either way. kStageOff,
-  // kStageOn (both block CTAs), or kStageAuto: the 256-thread CTA only, whose threads would
-  // otherwise load a block in two rounds (cells, then bed and halo), where the 512-thread CTA's
-  // one round is shorter than the copies' latency (256 x 256 a launch a tick: 7.2 against 7.5 us;
-  // 512 x 512: 11.8 against 11.7).
+  // takes each block's cells and halo by tensor copies, a CTA's next block's while it steps this
+  // one. The same bits either way. kStageOff, kStageOn (both block CTAs), or kStageAuto: a launch
+  // of 256-thread CTAs with more blocks than CTAs, where each CTA's next block's copies land while
+  // it steps the last and its threads would otherwise load a block in two rounds (1024 x 1024:
+  // 28.0 -> 29.1 Gcell/s). A CTA of one block (512 x 512: 11.7 against 11.8 us a tick) or one of
+  // 512 threads, which loads in one round (256 x 256: 7.1 against 7.5), is faster by its loads.
   static constexpr uint32_t kStageOff = 0, kStageOn = 1, kStageAuto = 2;
   void set_stage(uint32_t mode) { stage_ = mode; }
   uint32_t stage() const { return stage_; }
@@ -63,13 +64,16 @@ class TileSet {
   uint32_t staged_tiles() const { return staged_tiles_; }
   uint32_t staged_launch_tiles() const {
     if (shape_ != BlockShape::k32x16b) return 0u;
-    return stages(n_items_ <= uint32_t(sms_) ? BlockShape::k32x16w : shape_) ? staged_tiles_ : 0u;
+    const bool wide = n_items_ <= uint32_t(sms_);
+    return stages(wide ? BlockShape::k32x16w : shape_, n_items_, wide ? int(n_items_) + 1 : grid_)
+               ? staged_tiles_
+               : 0u;
   }
-  bool stages(BlockShape launch) const {
-    return staged_tiles_ > 0u &&
-           ((stage_ == kStageOn &&
-             (launch == BlockShape::k32x16b || launch == BlockShape::k32x16w)) ||
-            (stage_ == kStageAuto && launch == BlockShape::k32x16b));
+  // Whether a launch of this shape, items and grid takes the staged variant.
+  bool stages(BlockShape launch, uint32_t items, int grid) const {
+    if (staged_tiles_ == 0u) return false;
+    if (stage_ == kStageOn) return launch == BlockShape::k32x16b || launch == BlockShape::k32x16w;
+    return stage_ == kStageAuto && launch == BlockShape::k32x16b && items > uint32_t(grid);
   }
   // One tile's own tick (the per-tile-launch form): only that tile's work items.
   cudaError_t enqueue_tile_tick(cudaStream_t s, uint32_t tile, float max_dt);

@@ -211,7 +211,8 @@ class DeviceStep:
 
     def staged_tiles(self) -> int:
         """1 where the step's three-phase blocks take their cells and halo by tensor copies (a
-        width that is a multiple of 4, and 256-thread CTAs or WLCUDA_STAGE=1 at create), else 0."""
+        width that is a multiple of 4, and more blocks than the launch's 256-thread CTAs, or
+        WLCUDA_STAGE=1 at create), else 0."""
         return int(lib().wl_staged_tiles(self._h)) if self._h is not None else 0
 
     def run_steps(self, count: int, max_dt: float) -> bool:

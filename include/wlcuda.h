@@ -128,8 +128,9 @@ uint32_t wl_group_count(const wl_step* step);
 uint64_t wl_tick_launches(const wl_step* step);
 /* Tiles whose 32 x 16 blocks the step's launches take by tensor copies (no counterpart in the
  * reference: a diagnosis count): 1 where the tile's width is a multiple of 4 and the step ticks in
- * three-phase blocks of 256-thread CTAs (more blocks than SMs), or in either block CTA with
- * WLCUDA_STAGE=1 set at create (WLCUDA_STAGE=0: in neither); else 0. */
+ * three-phase blocks with more blocks than its launch's 256-thread CTAs (each CTA's next block's
+ * copies issued while it steps the current one), or in any block launch with WLCUDA_STAGE=1 set
+ * at create (WLCUDA_STAGE=0: in none); else 0. */
 uint32_t wl_staged_tiles(const wl_step* step);
 
 /* DeviceStep::write_state (water_live.cpp:271-314): each array n = nx * ny doubles, rounded to

@@ -1,11 +1,11 @@
 """The three-phase block tick's staged variant: each 32 x 16 block's cells and one-cell halo taken
 into shared memory by two tensor copies (TMA) in place of each thread's loads, for tiles whose width
-is a multiple of 4 (the default in the 256-thread block CTA; WLCUDA_STAGE=1 in the 512-thread one
-too). Held to the oracle bit for bit: a launch a tick on every case and flag, both forms of the
+is a multiple of 4. By default it runs where 256-thread block CTAs step blocks in turn, each CTA's
+next block's copies landing while it steps the last; WLCUDA_STAGE=1 turns it on in every block
+launch. Held to the oracle bit for bit: a launch a tick on every case and flag, both forms of the
 arithmetic; batches of uneven tiles (widths that take the copies beside widths that load cell by
-cell) in the 512-thread CTA (no more blocks than SMs) and the 256-thread one (many blocks a CTA,
-the copies of one block landing after the last one's faces); the tick queue, whose landed tiles
-skip their blocks."""
+cell) in the 512-thread CTA (no more blocks than SMs) and the 256-thread one (many blocks a CTA);
+the tick queue, whose landed tiles skip their blocks."""
 from __future__ import annotations
 
 import os
@@ -94,24 +94,29 @@ def stage_env(value):
 
 
 @pytest.mark.parametrize("env,want", [(None, 1), ("0", 0)])
-def test_the_default_stages_the_256_thread_blocks(gpu, env, want):
-    """A 400 x 300 tile (247 blocks, more than SMs: 256-thread block CTAs) stages by default and
-    not with WLCUDA_STAGE=0; a 256 x 256 tile (128 blocks: the 512-thread CTA) does not by default.
-    Both step to the oracle's bytes."""
-    n = 400 * 300
-    x, y = np.arange(n) % 400, np.arange(n) // 400
-    c = dict(nx=400, ny=300, cell_m=0.5, bed=0.002 * x + 0.001 * (y % 7),
-             h=np.where((x - 200) ** 2 + (y - 150) ** 2 < 900, 1.2, 0.05))
+def test_the_default_stages_blocks_a_cta_steps_in_turn(gpu, env, want):
+    """A 1024 x 512 tile (1024 blocks, more than the device's 256-thread CTAs: each CTA steps
+    blocks in turn, the next one's copies landing while it steps the last) stages by default and
+    not with WLCUDA_STAGE=0. A 512 x 512 tile (512 blocks, a CTA each) and a 256 x 256 one (128
+    blocks: the 512-thread CTA) do not by default. The staged tile steps to the oracle's bytes."""
+    nx, ny = 1024, 512
+    n = nx * ny
+    x, y = np.arange(n) % nx, np.arange(n) // nx
+    c = dict(nx=nx, ny=ny, cell_m=0.5, bed=0.002 * x + 0.001 * (y % 7),
+             h=np.where((x - 500) ** 2 + (y - 250) ** 2 < 2500, 1.2, 0.05))
     with stage_env(env):
         dev, ref = make_pair(c, rows=1)
-        small, _ = make_pair(lake_256(), rows=1)
+        others = [make_pair(lake_256(), rows=1)[0],
+                  make_pair(dict(nx=512, ny=512, cell_m=0.5, bed=np.zeros(512 * 512),
+                                 h=np.full(512 * 512, 0.3)), rows=1)[0]]
     assert dev.staged_tiles() == want
-    assert small.staged_tiles() == 0
-    small.destroy()
-    for _ in range(15):
+    for o in others:
+        assert o.staged_tiles() == 0
+        o.destroy()
+    for _ in range(12):
         assert dev.run_steps(1, 0.02), dev.error
-    ref.run_steps(15, 0.02)
-    assert_same(dev, ref, f"400 x 300, WLCUDA_STAGE={env}")
+    ref.run_steps(12, 0.02)
+    assert_same(dev, ref, f"{nx} x {ny}, WLCUDA_STAGE={env}")
     dev.destroy()
 
 
@@ -153,9 +158,9 @@ def test_staged_mixed_tiles_equal_their_oracles(gpu, graph):
 
 def test_staged_many_blocks_a_cta(gpu):
     """The batched configuration's tiles (dry land, a column each), more blocks than SMs: the
-    256-thread CTA steps many blocks in turn, each block's copies issued after the CTA's last
-    block's faces are read. Every tile equals the unstaged blocks' bytes after 120 ticks, and
-    sampled tiles the oracle's."""
+    256-thread CTA steps many blocks in turn, each next block's copies issued once the last
+    block's reads of the stage are done. Every tile equals the unstaged blocks' bytes after 120
+    ticks, and sampled tiles the oracle's."""
     from test_batch_gpu import load, oracle_tile
     from game_engine_gb300 import workloads
     from game_engine_gb300.batch import Batch
