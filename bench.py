@@ -369,8 +369,8 @@ def run_plain(args, tile, rank, world):
 def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
     """The batched configuration: `count` tiles of seeded uneven sides, `ticks` ticks a step, one
     persistent CUDA-graph-captured launch a tick after the autotuner's choice; beside it the
-    per-tile-launch form (one launch per tile per tick) on the same tiles, its best of three
-    launch strategies."""
+    per-tile-launch form (one launch per tile per tick) on the same tiles, its best of five
+    launch forms."""
     import torch
     from game_engine_gb300 import workloads
     from game_engine_gb300.batch import Batch, concat
@@ -407,16 +407,17 @@ def run_tiles(steps: int, warmup: int, ticks: int = 0, count: int = 4096):
         hashes_equal = got == gold["hashes"]
         assert hashes_equal, (f"{sum(a != w for a, w in zip(got, gold['hashes']))} of {count} "
                               "tiles differ from the oracle's hashes")
-    # The per-tile-launch form on the same tiles, timed four ways: 16-row marches on one stream,
+    # The per-tile-launch form on the same tiles, timed five ways: 16-row marches on one stream,
     # from a captured graph, and dealt to 64 concurrent streams as independent steps would run;
-    # and the three-phase blocks (the small-tile shape) on 64 streams. The best of them is the
-    # comparison. Fewer ticks: it is slow.
+    # and the three-phase blocks (the small-tile shape) on 64 streams, with their loads and staged
+    # by tensor copies. The best of them is the comparison. Fewer ticks: it is slow.
     per_ticks = 10
     per = {}
-    for name, graph, nstreams, rows in (("stream", False, 1, 16), ("graph", True, 1, 16),
-                                        ("streams_64", False, 64, 16),
-                                        ("streams_64_blocks", False, 64, 1)):
-        b.set_tuning(rows, 0)
+    for name, graph, nstreams, rows, stage in (
+            ("stream", False, 1, 16, 0), ("graph", True, 1, 16, 0),
+            ("streams_64", False, 64, 16, 0), ("streams_64_blocks", False, 64, 1, 0),
+            ("streams_64_blocks_staged", False, 64, 1, 1)):
+        b.set_tuning(rows, 0, stage=stage)
         b.write_state(h0)
         b.run_tile_ticks(2, workloads.MAX_DT, graph=graph, streams=nstreams)
         ev[0].record(stream)
