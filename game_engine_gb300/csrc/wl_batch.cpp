@@ -39,9 +39,11 @@ struct wl_batch {
   uint32_t graph_ticks = 0;
   float graph_max_dt = 0.0f;
   uint64_t graph_key = 0;
+  uint32_t graph_checks = 0;  // the device words its launches set (TileSet::pending_checks)
   cudaGraphExec_t tile_graph = nullptr;
   float tile_graph_max_dt = 0.0f;
   uint64_t tile_graph_key = 0;
+  uint32_t tile_graph_checks = 0;
   std::vector<cudaStream_t> side_streams;  // the per-tile form's concurrent streams
   ~wl_batch() {
     if (graph != nullptr) cudaGraphExecDestroy(graph);
@@ -381,10 +383,12 @@ int wl_batch_run_ticks(wl_batch* b, uint32_t count, float max_dt, int use_graph,
       b->graph_ticks = g;
       b->graph_max_dt = max_dt;
       b->graph_key = key;
+      b->graph_checks = b->set.pending_checks();
     }
     while (left >= b->graph_ticks) {
       if (cudaGraphLaunch(b->graph, st) != cudaSuccess)
         return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaGraphLaunch");
+      b->set.add_checks(b->graph_checks);
       left -= b->graph_ticks;
     }
   }
@@ -459,10 +463,13 @@ int wl_batch_run_tile_ticks(wl_batch* b, uint32_t count, float max_dt, int use_g
       cudaGraphDestroy(graph);
       b->tile_graph_max_dt = max_dt;
       b->tile_graph_key = key;
+      b->tile_graph_checks = b->set.pending_checks();
     }
-    for (uint32_t k = 0; k < count; ++k)
+    for (uint32_t k = 0; k < count; ++k) {
       if (cudaGraphLaunch(b->tile_graph, st) != cudaSuccess)
         return fail(err, err_len, WL_ERR_CUDA, "water_live: cudaGraphLaunch");
+      b->set.add_checks(b->tile_graph_checks);
+    }
   } else {
     for (uint32_t k = 0; k < count; ++k)
       for (uint32_t t = 0; t < n; ++t)

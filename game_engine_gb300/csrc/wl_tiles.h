@@ -60,6 +60,17 @@ class TileSet {
   static constexpr uint32_t kStageOff = 0, kStageOn = 1, kStageAuto = 2;
   void set_stage(uint32_t mode) { stage_ = mode; }
   uint32_t stage() const { return stage_; }
+  // The device words wait() reads after the launches since the last wait: the resident tick's
+  // barrier error word and the staged tick's fault word. A captured graph keeps the ones its
+  // launches set (pending_checks after the capture) and adds them at each replay (add_checks).
+  static constexpr uint32_t kCheckResident = 1, kCheckStage = 2;
+  uint32_t pending_checks() const {
+    return (resident_used_ ? kCheckResident : 0u) | (stage_used_ ? kCheckStage : 0u);
+  }
+  void add_checks(uint32_t checks) {
+    resident_used_ = resident_used_ || (checks & kCheckResident) != 0u;
+    stage_used_ = stage_used_ || (checks & kCheckStage) != 0u;
+  }
   // Tiles with tensor maps (the staged variant's tiles), and those the set's launches stage.
   uint32_t staged_tiles() const { return staged_tiles_; }
   uint32_t staged_launch_tiles() const {

@@ -49,6 +49,34 @@ CASES = {
 }
 
 
+def narrow():
+    """32 x 20: narrower than a copy's box (40 columns) and shorter than it (18 rows), so every
+    box reaches past the tile on both sides."""
+    n = 32 * 20
+    x, y = np.arange(n) % 32, np.arange(n) // 32
+    return dict(nx=32, ny=20, cell_m=0.5, bed=0.01 * x + 0.02 * (y % 3),
+                h=np.where(x < 10, 0.5, 0.05), open_edges=6)
+
+
+SMALL = {"narrow": narrow, "dam_1d": lambda: cases.dam(400, 0.001)}
+
+
+@pytest.mark.parametrize("name", sorted(SMALL))
+def test_staged_tiles_smaller_than_a_box(gpu, name):
+    """Tiles smaller than a copy's box: where the driver's encoder gives them tensor maps, the
+    copies' cells past the tile arrive as zeros and are not read; either way, the oracle's bytes."""
+    c = SMALL[name]()
+    with staged():
+        dev, ref = make_pair(c, rows=1)
+    assert dev.staged_tiles() in (0, 1)
+    print(f"{name}: staged_tiles {dev.staged_tiles()}")
+    for _ in range(29):
+        assert dev.run_steps(1, 0.01), dev.error
+    ref.run_steps(29, 0.01)
+    assert_same(dev, ref, name)
+    dev.destroy()
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
 @pytest.mark.parametrize("fixed", [False, True])
 def test_staged_launch_a_tick_equals_the_oracle(gpu, name, fixed):
