@@ -94,8 +94,8 @@ def test_tiles_256_adjoint_losses_and_gradients(gpu):
                 worst = max(worst, err)
                 assert err < ADJOINT_TOL, (k, key, where, err)
     print(f"tiles_256_adjoint: worst gradient error {worst:.2e} of each tile's largest")
-    # Against the FP64 replay's central differences on four tiles (the benchmark spec's bound, 1e-4
-    # of the largest difference at the tile's cells).
+    # Against the FP64 replay's central differences on four tiles (the adjoint's bound, 1e-4 of
+    # the largest difference at the tile's cells).
     from adjoint_cases import rel_err
     for r in golden()["tiles_256_adjoint_fd"]:
         k = r["index"]
